@@ -1,0 +1,201 @@
+"""ctypes mirror of include/fivonagi.h and the loader of libfivonagi.so.
+
+The library is the product: a C ABI over hand-written sm_103a kernels. This
+module only declares its types and entry points; it never computes anything
+itself, and loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libfivonagi.so")
+
+# fv_status (include/fivonagi.h)
+FV_OK = 0
+FV_DT_TOO_LARGE = 1
+FV_NEGATIVE_EIGENVALUE = 2
+FV_TRANSONIC = 3
+FV_COLLECT_OVERFLOW = 4
+FV_TIMEOUT = 5
+FV_CUDA_ERROR = 6
+FV_BAD_ARG = 7
+FV_NO_DEVICE = 8
+
+STATUS_NAMES = {
+    FV_OK: "ok",
+    FV_DT_TOO_LARGE: "dt too large",
+    FV_NEGATIVE_EIGENVALUE: "negative eigenvalue",
+    FV_TRANSONIC: "transonic rarefaction",
+    FV_COLLECT_OVERFLOW: "data collection overflow",
+    FV_TIMEOUT: "device wait timed out",
+    FV_CUDA_ERROR: "CUDA error",
+    FV_BAD_ARG: "bad argument",
+    FV_NO_DEVICE: "no usable device",
+}
+
+# fv_app
+FV_APP_HIFU_BEAM = 0
+FV_APP_TAYLOR_ANGLE_XY = 1
+FV_APP_PLANE_WAVE = 2
+FV_APP_FOCUSED_BEAM = 3
+APP_NAMES = {
+    "hifu-beam": FV_APP_HIFU_BEAM,
+    "taylor-angle-xy": FV_APP_TAYLOR_ANGLE_XY,
+    "plane-wave": FV_APP_PLANE_WAVE,
+    "focused-beam": FV_APP_FOCUSED_BEAM,
+}
+
+# fv_stage
+FV_STAGE_BOUNDARY = 0
+FV_STAGE_SWEEP_Y = 1
+FV_STAGE_SWEEP_X = 2
+FV_STAGE_SOURCE = 3
+
+
+class FvParams(C.Structure):
+    _fields_ = [
+        ("app", C.c_int32),
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("cfl_even_only", C.c_int32),
+        ("moving_domain", C.c_int32),
+        ("exact", C.c_int32),
+        ("max_retries", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("xmax", C.c_double),
+        ("ymax", C.c_double),
+        ("beta", C.c_double),
+        ("diffdelta", C.c_double),
+        ("cflmax", C.c_double),
+        ("cflwhish", C.c_double),
+        ("dtini", C.c_double),
+        ("tide", C.c_double),
+        ("mdvx", C.c_double),
+        ("mdvy", C.c_double),
+        ("mdt", C.c_double),
+        ("ampl", C.c_double),
+        ("frec", C.c_double),
+        ("angle", C.c_double),
+        ("isp_a", C.c_double),
+        ("isp_f", C.c_double),
+        ("isp_rhoa", C.c_double),
+        ("isp_c", C.c_double),
+        ("aperture", C.c_double),
+        ("center", C.c_double),
+        ("ramp_periods", C.c_double),
+    ]
+
+    def copy(self) -> "FvParams":
+        out = FvParams()
+        C.pointer(out)[0] = self
+        return out
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+    def replace(self, **kw) -> "FvParams":
+        out = self.copy()
+        for k, v in kw.items():
+            if not hasattr(out, k):
+                raise AttributeError(f"fv_params has no field {k!r}")
+            setattr(out, k, v)
+        return out
+
+
+class FvRunStats(C.Structure):
+    _fields_ = [
+        ("accepted", C.c_int64),
+        ("rejected", C.c_int64),
+        ("dt", C.c_double),
+        ("T", C.c_double),
+        ("cfl", C.c_double),
+        ("n", C.c_int32),
+        ("status", C.c_int32),
+        ("mdx", C.c_int32),
+        ("mdy", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_P = C.c_void_p
+_FP = C.POINTER(C.c_float)
+
+# name -> (restype, argtypes); every entry point declared in include/fivonagi.h
+PROTOTYPES = {
+    "fv_version": (C.c_char_p, []),
+    "fv_last_error_string": (C.c_char_p, []),
+    "fv_default_params": (C.c_int, [C.c_int32, C.POINTER(FvParams)]),
+    "fv_create": (C.c_int, [C.POINTER(FvParams), C.POINTER(_P)]),
+    "fv_destroy": (C.c_int, [_P]),
+    "fv_init_state": (C.c_int, [_P]),
+    "fv_set_state": (C.c_int, [_P, _P, _P, _P, C.c_int32]),
+    "fv_get_state": (C.c_int, [_P, _P, _P, _P, C.c_int32]),
+    "fv_set_scalars": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
+    "fv_get_stats": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_set_stream": (C.c_int, [_P, _P]),
+    "fv_run": (C.c_int, [_P, C.c_int64, C.POINTER(FvRunStats)]),
+    "fv_run_until": (C.c_int, [_P, C.c_double, C.POINTER(FvRunStats)]),
+    "fv_launch_attempts": (C.c_int, [_P, C.c_int64]),
+    "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
+}
+
+_lib = None
+
+
+class FvError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        name = STATUS_NAMES.get(status, f"status {status}")
+        msg = f"{where}: {name}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load libfivonagi.so and declare its prototypes.
+
+    Raises FileNotFoundError when the library is missing: there is no
+    fallback path.
+    """
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+        )
+    lib = C.CDLL(p)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int, where: str) -> None:
+    if status != FV_OK:
+        detail = ""
+        if _lib is not None:
+            raw = _lib.fv_last_error_string()
+            detail = raw.decode() if raw else ""
+        raise FvError(status, where, detail)
+
+
+def default_params(app: int | str) -> FvParams:
+    """The app's reference parameter values (its parameters.h), from the library."""
+    if isinstance(app, str):
+        app = APP_NAMES[app]
+    lib = load_library()
+    p = FvParams()
+    check(lib.fv_default_params(app, C.byref(p)), "fv_default_params")
+    return p

@@ -1,0 +1,181 @@
+/*
+ * fivonagi.h -- C ABI of the GB300 (sm_103a) FiVoNAGI time-step hot path.
+ *
+ * One step of the 2-D nonlinear, dissipative acoustics solver:
+ *   boundary forcing (app hook) -> y sweep -> x sweep -> CFL max-reduction
+ *   -> (step accepted) fractional velocity diffusion, T += dt -> dt update.
+ *
+ * The reference composes this step out of ~34 kernels and 7 blocking
+ * device-to-host copies per step (common/main.cu:310-635). Here one fused
+ * kernel launch performs the whole step, the accept/reject decision and the
+ * dt update happen on the device, and the host synchronises only when a
+ * call returns.
+ *
+ * Plain C types only: no CUDA or torch types cross this boundary. All calls
+ * return an fv_status; none of them exits the process (the reference calls
+ * exit() on every error, common/main.cu:365-368, 600-609,
+ * common/debug_tools.h:44-55).
+ *
+ * State layout: three FP32 fields u1 = rho-1, u2 = rho*vx, u3 = rho*vy,
+ * each NX*NY, row-major with i (x, axial) fastest: offset = i + j*NX, the
+ * reference's layout (apps/na/fv.h:15-17).
+ */
+#ifndef FIVONAGI_H
+#define FIVONAGI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FV_ABI_VERSION 1
+
+/* Status codes. 1, 2, 3, 4 are the reference's simError values
+ * (common/data_definitions.h:78-83); the rest are the library's own. */
+typedef enum fv_status {
+  FV_OK = 0,
+  FV_DT_TOO_LARGE = 1,        /* CFL >= CFLMAX on every retry of a step (max_retries) */
+  FV_NEGATIVE_EIGENVALUE = 2, /* a Riemann solve met tmp3 < 0 (apps/na/fv.h:102, 290) */
+  FV_TRANSONIC = 3,           /* declared by the reference, never raised; reserved */
+  FV_COLLECT_OVERFLOW = 4,    /* reserved for data collection */
+  FV_TIMEOUT = 5,             /* a bounded device wait ran out */
+  FV_CUDA_ERROR = 6,          /* a CUDA runtime call failed; see fv_last_error_string */
+  FV_BAD_ARG = 7,             /* invalid argument; see fv_last_error_string */
+  FV_NO_DEVICE = 8            /* no usable sm_103 device */
+} fv_status;
+
+/* Per-app plugins. The reference selects one app per build through
+ * include-guard shadowing of parameters.h / init.h / boundary.h
+ * (apps/hifu-beam/driver.cu:40-52); here the app is a runtime choice and
+ * each app's boundary hook is a device functor fused into the step kernel. */
+typedef enum fv_app {
+  FV_APP_HIFU_BEAM = 0,       /* apps/hifu-beam: focused pulsed source, reflecting axis */
+  FV_APP_TAYLOR_ANGLE_XY = 1, /* apps/taylor-angle-xy: analytic tanh (Taylor shock) ghosts */
+  FV_APP_PLANE_WAVE = 2,      /* oblique sinusoidal plane wave, no-flux y walls */
+  FV_APP_FOCUSED_BEAM = 3     /* focused continuous-wave source, open boundaries */
+} fv_app;
+
+/* Run-time parameter block. Names follow the reference's parameters.h
+ * constants (apps/hifu-beam/parameters.h:12-104,
+ * apps/taylor-angle-xy/parameters.h:12-109). Values are double; the solver
+ * rounds each to FP32 once, as the reference's `static const DATATYPEV`
+ * definitions do at PRECISION=1. */
+typedef struct fv_params {
+  int32_t app;            /* fv_app */
+  int32_t nx, ny;         /* NX, NY: grid cells (any size >= 8; the reference needs powers of 2) */
+  int32_t cfl_even_only;  /* 1: CFL max over even flat offsets only, the reference's
+                             pairwise reduction stopping at 2 (common/main.cu:503-519) */
+  int32_t moving_domain;  /* 1: shift the window once T >= MDT (common/main.cu:109-177) */
+  int32_t exact;          /* 1: no FMA contraction (bit-identical to the oracle);
+                             0: contracted FMAs (within the FP32 tolerance) */
+  int32_t max_retries;    /* consecutive rejected attempts before FV_DT_TOO_LARGE */
+  int32_t reserved0;
+  double xmax, ymax;      /* XMAX, YMAX: dx = XMAX/(NX-1), dy = YMAX/(NY-1) (common/main.cu:790-791) */
+  double beta;            /* BETA: nonlinearity coefficient */
+  double diffdelta;       /* DIFFDELTA: dimensionless dissipation */
+  double cflmax;          /* CFLMAX: steps with CFL >= CFLMAX are rejected */
+  double cflwhish;        /* CFLWHISH: target CFL for the next dt */
+  double dtini;           /* DTINI: dt of the first step */
+  double tide;            /* TIDE: T starts at -TIDE */
+  double mdvx, mdvy, mdt; /* MDVX, MDVY, MDT: moving-domain velocity and start time */
+  /* app block */
+  double ampl;            /* AMPL: source amplitude (Mach) */
+  double frec;            /* FREC: source frequency (1/lambda) */
+  double angle;           /* ISPTHETA (taylor) / propagation angle (plane wave), radians */
+  double isp_a;           /* hifu ISPa: source aperture, lambda units */
+  double isp_f;           /* hifu ISPF, focused-beam focal distance: in grid points */
+  double isp_rhoa;        /* taylor ISPRHOA */
+  double isp_c;           /* taylor ISPC */
+  double aperture;        /* focused beam: aperture width, cells */
+  double center;          /* focused beam: aperture centre, j index */
+  double ramp_periods;    /* focused beam: linear amplitude ramp length, periods */
+} fv_params;
+
+typedef struct fv_run_stats {
+  int64_t accepted;       /* accepted steps in the call */
+  int64_t rejected;       /* rejected attempts in the call */
+  double dt;              /* dt for the next step */
+  double T;               /* simulation time */
+  double cfl;             /* CFL of the last attempted step */
+  int32_t n;              /* total accepted steps since the state was set */
+  int32_t status;         /* fv_status of the device run */
+  int32_t mdx, mdy;       /* moving-domain offsets MDX, MDY */
+} fv_run_stats;
+
+/* Stages for fv_debug_step: the state after each phase of one step. */
+typedef enum fv_stage {
+  FV_STAGE_BOUNDARY = 0,  /* ghost cells rewritten (the app's boundary hook) */
+  FV_STAGE_SWEEP_Y = 1,   /* after getWavesSpeedsCFL_y/step_y/calcLimiters_y/writeLimiters_y */
+  FV_STAGE_SWEEP_X = 2,   /* after the x sweep */
+  FV_STAGE_SOURCE = 3     /* after the diffusion step (source) */
+} fv_stage;
+
+typedef struct fv_handle fv_handle;
+
+/* Library identification and the last error message of the calling thread. */
+const char *fv_version(void);
+const char *fv_last_error_string(void);
+
+/* Fill *out with the app's reference parameter values.
+ * Replaces the compile-time parameters.h of each app
+ * (apps/hifu-beam/parameters.h:12-104, apps/taylor-angle-xy/parameters.h:12-109). */
+fv_status fv_default_params(int32_t app, fv_params *out);
+
+/* Allocate device state for one simulation on the current CUDA device.
+ * Replaces gpu_init (common/data_definitions.h:523-871). */
+fv_status fv_create(const fv_params *p, fv_handle **out);
+
+/* Free everything fv_create allocated. Replaces clean_gpu
+ * (common/data_definitions.h:415-517). */
+fv_status fv_destroy(fv_handle *h);
+
+/* Run the app's initial-value hook (host side, as the reference's init<TTT>,
+ * apps/hifu-beam/init.h:16-25, apps/taylor-angle-xy/init.h:19-27), upload
+ * it, and reset dt = DTINI, T = -TIDE, n = 0, MDX = MDY = 0
+ * (common/main.cu:789-795, 807-815). */
+fv_status fv_init_state(fv_handle *h);
+
+/* Copy a state in or out. on_device = 0: host pointers; 1: device pointers
+ * on the handle's device. Each pointer addresses NX*NY floats.
+ * fv_set_state also resets dt, T, n, MDX, MDY as fv_init_state does. */
+fv_status fv_set_state(fv_handle *h, const float *u1, const float *u2,
+                       const float *u3, int32_t on_device);
+fv_status fv_get_state(fv_handle *h, float *u1, float *u2, float *u3,
+                       int32_t on_device);
+
+/* Set or read the scalar time-stepping state (dt, T, n). */
+fv_status fv_set_scalars(fv_handle *h, double dt, double T, int32_t n);
+fv_status fv_get_stats(fv_handle *h, fv_run_stats *out);
+
+/* Use a caller-provided cudaStream_t (passed as void*); NULL = the
+ * library's own stream. */
+fv_status fv_set_stream(fv_handle *h, void *cuda_stream);
+
+/* Advance by exactly nsteps accepted steps (rejected attempts are retried
+ * with the reduced dt and counted). The inner loop of calcFrame
+ * (common/main.cu:310-635) without its per-step host synchronisation. */
+fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out);
+
+/* Advance until T >= t_stop, the calcFrame loop condition `while (T < Tprint)`
+ * (common/main.cu:310). */
+fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out);
+
+/* Enqueue nattempts step attempts on the handle's stream and return without
+ * synchronising (accepted and rejected attempts both count). For timing
+ * loops; pair with fv_sync. */
+fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts);
+fv_status fv_sync(fv_handle *h, fv_run_stats *out);
+
+/* One step of the current state, stopped after `stage`; writes the stage's
+ * full grid to u1/u2/u3 (host pointers) and leaves the handle's state,
+ * dt, T and n unchanged. For per-phase parity tests. */
+fv_status fv_debug_step(fv_handle *h, int32_t stage, float *u1, float *u2,
+                        float *u3);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FIVONAGI_H */

@@ -1,0 +1,167 @@
+"""ctypes loader for the oracle libraries. TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use
+this module, as the checker and the CPU baseline; the product package
+(fivonagi_gb300) never imports it.
+
+  OracleSim  -- the CPU restatement (oracle/fv_oracle.cpp, built into
+                oracle/_build/liboracle.so), FP32 or FP64.
+  ref_run    -- the reference's own headers built on the host through
+                oracle/ref_shim.cpp (oracle/_ref/libfvref.so); exists only
+                where the reference tree was present at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from fivonagi_gb300._abi import FvParams, FvRunStats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libfvref.so")
+REF_ROOT_DEFAULT = "/root/reference"
+
+REF_APP_KEYS = {0: "hifu", 1: "taylor", 2: "plane", 3: "focused"}
+
+_oracle = None
+_ref = None
+
+
+def build_oracle(ref_root: str | None = None, with_ref: bool = True) -> None:
+    """Compile the restatement, and the reference shim when its tree exists."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    root = ref_root or REF_ROOT_DEFAULT
+    if with_ref and os.path.isdir(os.path.join(root, "apps", "na")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF_ROOT={root}"], check=True)
+
+
+def _load_oracle() -> C.CDLL:
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_LIB):
+            build_oracle(with_ref=False)
+        lib = C.CDLL(ORACLE_LIB)
+        P = C.c_void_p
+        lib.fvo_create.restype = P
+        lib.fvo_create.argtypes = [C.POINTER(FvParams), C.c_int]
+        lib.fvo_destroy.argtypes = [P]
+        lib.fvo_set_threads.restype = C.c_int
+        lib.fvo_set_threads.argtypes = [C.c_int]
+        for name in ("fvo_init_state",):
+            getattr(lib, name).argtypes = [P]
+        lib.fvo_set_state.argtypes = [P, P, P, P]
+        lib.fvo_get_state.argtypes = [P, P, P, P]
+        lib.fvo_set_scalars.argtypes = [P, C.c_double, C.c_double, C.c_int]
+        lib.fvo_get_stats.argtypes = [P, C.POINTER(FvRunStats)]
+        lib.fvo_run.argtypes = [P, C.c_int64, C.POINTER(FvRunStats)]
+        lib.fvo_debug_step.argtypes = [P, C.c_int, P, P, P]
+        lib.fvo_last_cfl.restype = C.c_double
+        lib.fvo_last_cfl.argtypes = [P]
+        _oracle = lib
+    return _oracle
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _load_ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise FileNotFoundError(f"{REF_LIB} not built (needs the reference tree)")
+        _ref = C.CDLL(REF_LIB)
+    return _ref
+
+
+def set_threads(n: int) -> int:
+    return _load_oracle().fvo_set_threads(int(n))
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class OracleSim:
+    """One simulation of the CPU restatement, mirroring the C ABI's handle."""
+
+    def __init__(self, params: FvParams, dtype=np.float32):
+        self.lib = _load_oracle()
+        self.params = params.copy()
+        self.dtype = np.dtype(dtype)
+        prec = self.dtype.itemsize
+        self.h = self.lib.fvo_create(C.byref(self.params), prec)
+        if not self.h:
+            raise ValueError("oracle rejected the parameters")
+        self.shape = (params.ny, params.nx)
+
+    def close(self):
+        if self.h:
+            self.lib.fvo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_state(self):
+        self.lib.fvo_init_state(self.h)
+
+    def set_state(self, u1, u2, u3):
+        arrs = [np.ascontiguousarray(u, dtype=self.dtype).reshape(self.shape) for u in (u1, u2, u3)]
+        self.lib.fvo_set_state(self.h, *[_ptr(a) for a in arrs])
+
+    def get_state(self):
+        out = [np.empty(self.shape, self.dtype) for _ in range(3)]
+        self.lib.fvo_get_state(self.h, *[_ptr(a) for a in out])
+        return out
+
+    def set_scalars(self, dt, T, n=0):
+        self.lib.fvo_set_scalars(self.h, float(dt), float(T), int(n))
+
+    def stats(self) -> dict:
+        st = FvRunStats()
+        self.lib.fvo_get_stats(self.h, C.byref(st))
+        return st.as_dict()
+
+    def run(self, nsteps: int) -> dict:
+        st = FvRunStats()
+        rc = self.lib.fvo_run(self.h, int(nsteps), C.byref(st))
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
+    def debug_step(self, stage: int):
+        out = [np.empty(self.shape, self.dtype) for _ in range(3)]
+        rc = self.lib.fvo_debug_step(self.h, int(stage), *[_ptr(a) for a in out])
+        return rc, out
+
+    def last_cfl(self) -> float:
+        return self.lib.fvo_last_cfl(self.h)
+
+
+def ref_call(params: FvParams, op: int, u, dtype=np.float32, nsteps: int = 0, scalars=None):
+    """Call the reference shim: op 0 init, 1 run nsteps, 10+stage debug step.
+
+    `u` is a list of three (ny, nx) arrays (updated in place); scalars is
+    [dt, T, n, MDX, MDY] (updated in place). Returns (status, stats dict).
+    """
+    lib = _load_ref()
+    key = REF_APP_KEYS[int(params.app)]
+    suffix = "f32" if np.dtype(dtype) == np.float32 else "f64"
+    fn = getattr(lib, f"fvref_{key}_{suffix}")
+    fn.restype = C.c_int
+    fn.argtypes = [C.POINTER(FvParams), C.c_int, C.c_int64, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.POINTER(FvRunStats)]
+    if scalars is None:
+        scalars = np.array([params.dtini, -params.tide, 0, 0, 0], np.float64)
+    st = FvRunStats()
+    p = params.copy()
+    rc = fn(C.byref(p), int(op), int(nsteps), *[_ptr(a) for a in u], _ptr(scalars), C.byref(st))
+    return rc, st.as_dict()
