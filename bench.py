@@ -1,0 +1,379 @@
+"""Benchmark of the fused time-step kernel on the headline workload.
+
+Workload (the reference's headline plain-method case at full size): the
+focused-beam app on a 4096 (axial) x 2048 (lateral) FP32 grid, 24 cells per
+wavelength, aperture 1024 cells, focus 3000 cells, Mach 5e-3 reached over 5
+periods, beta 3.5, dissipation 5e-5, CFL 0.9. Synthetic: the state starts at
+rest and the source drives it; no dataset is involved.
+
+One bench step = one accepted time step of the whole grid (boundary hook,
+y and x sweeps, CFL reduction and dt control, diffusion).
+
+  value : Gcell-updates/s over K back-to-back steps, device-timed with CUDA
+          events on the solver's stream, state resident in HBM.
+  e2e   : the same metric through the C ABI a user calls, with host buffers:
+          fv_set_state from pinned host memory, K synchronous fv_run(1)
+          calls (each returns the step's stats: dt, T, CFL, status), and
+          fv_get_state back to pinned host memory, all inside the timed
+          region.
+  roofline : the step kernel against the measured HBM copy bandwidth, with
+          24 algorithmic bytes per cell-update (3 FP32 fields read once and
+          written once).
+  cpu_baseline : the oracle's CPU restatement (FP32, OpenMP over rows, all
+          host cores) on a bounded sample of the same grid.
+
+`--impl reference` times that CPU restatement alone (the reference's GPU
+code cannot be built with current toolkits; its arithmetic runs on the host
+through the restatement) and prints the same line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+ALG_BYTES_PER_CELL = 24  # 3 FP32 fields read + 3 written
+L2_BYTES = 129 * 1024 * 1024
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "step_kernel_focused_beam_4096x2048.traffic.json")
+
+
+def workload_params(exact: bool):
+    from fivonagi_gb300 import FV_APP_FOCUSED_BEAM, default_params
+    return default_params(FV_APP_FOCUSED_BEAM).replace(exact=1 if exact else 0)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "power_w_max": max(power) if power else None,
+            "samples": len(sm),
+            "reasons": sorted(reasons),
+        }
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            d = json.load(f)
+        return d.get("bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_sample(params, seconds: float, max_steps: int):
+    """The oracle (FP32 CPU restatement) on the full grid, bounded in time."""
+    import numpy as np
+
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    sim = oracle.OracleSim(params, np.float32, math="fvm")
+    sim.init_state()
+    sim.run(1)  # warm-up: first touch of the scratch grids
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < seconds:
+        sim.run(1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    sim.close()
+    cells = params.nx * params.ny
+    return {
+        "value": cells * steps / dt / 1e9,
+        "unit": "Gcell-updates/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{steps} accepted steps of the full {params.nx}x{params.ny} grid from rest "
+                  f"({dt:.1f} s, FP32, OpenMP over rows)",
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    params = workload_params(exact=True)
+    res = cpu_sample(params, seconds=25.0, max_steps=max(1, args.steps))
+    line = {
+        "impl": "reference",
+        "metric": "Gcell-updates/s",
+        "value": res["value"],
+        "unit": "Gcell-updates/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "focused-beam 4096x2048 FP32 (plain method, full size)",
+                   "nx": params.nx, "ny": params.ny, "runs": "CPU restatement of the reference "
+                   "arithmetic on the host cores (the reference's CUDA does not build on current toolkits)"},
+        "cpu_baseline": {"kind": res["kind"], "cores": res["cores"], "sample": res["sample"],
+                         "value": res["value"], "unit": res["unit"]},
+        "e2e": {"value": res["value"], "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from fivonagi_gb300 import Simulation, _abi
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    exact = not args.fast
+    params = workload_params(exact)
+    cells = params.nx * params.ny
+
+    # ---- device-timed throughput (state resident in HBM)
+    sim = Simulation(params)
+    sim.init_state()
+    stream = torch.cuda.Stream(device=dev)
+    sim.set_stream(stream.cuda_stream)
+    if args.warmup:
+        sim.run(args.warmup)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.launch_attempts(args.steps)
+    ev1.record(stream)
+    stream.synchronize()
+    st = sim.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    accepted = int(st["accepted"])
+    value = cells * accepted * world / (ms * 1e-3) / 1e9
+    per_launch_ms = ms / max(1, accepted + int(st["rejected"]))
+
+    # ---- one step timed alone after an L2 flush, as a cross-check
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    flushed = []
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.launch_attempts(1)
+        e1.record(stream)
+        stream.synchronize()
+        flushed.append(e0.elapsed_time(e1))
+    sim.sync()
+    del flush
+    flushed_ms = statistics.median(flushed)
+    sim.close()
+
+    # ---- end to end through the C ABI with pinned host buffers
+    sim = Simulation(params)
+    sim.set_stream(stream.cuda_stream)
+    u0 = torch.zeros((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
+    u_out = torch.empty((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
+    lib = sim.lib
+    stats = _abi.FvRunStats()
+    e2e_steps = min(args.steps, args.e2e_steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _abi.check(lib.fv_set_state(sim.h, u0[0].data_ptr(), u0[1].data_ptr(), u0[2].data_ptr(), 0), "set_state")
+    for _ in range(e2e_steps):
+        _abi.check(lib.fv_run(sim.h, 1, C.byref(stats)), "fv_run")
+    _abi.check(lib.fv_get_state(sim.h, u_out[0].data_ptr(), u_out[1].data_ptr(), u_out[2].data_ptr(), 0),
+               "get_state")
+    t1 = time.perf_counter()
+    sim.close()
+    e2e_s = t1 - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    state_bytes = 3 * cells * 4
+    ctrl_bytes = C.sizeof(_abi.FvRunStats)
+    e2e = {
+        "value": cells * e2e_steps * world / e2e_s / 1e9,
+        "unit": "Gcell-updates/s",
+        "steps": e2e_steps,
+        "h2d_bytes_per_step": state_bytes / e2e_steps,
+        "d2h_bytes_per_step": state_bytes / e2e_steps + 88,
+        "calls": "fv_set_state(pinned host) + steps x fv_run(1) (sync, stats read back) + fv_get_state(pinned host)",
+    }
+    del ctrl_bytes
+
+    peak, peak_kind = measured_peak()
+    alg_bytes = ALG_BYTES_PER_CELL * cells
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = profiled_traffic()
+    roofline = {
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "peak_source": f"hbm_gbs, {peak_kind} (MEASURED_PEAKS.json)",
+        "traffic": traffic,
+        "kernel": "step_kernel (fused y/x sweeps, CFL, diffusion)",
+        "bytes_per_launch": alg_bytes,
+        "launch_ms": per_launch_ms,
+        "launch_ms_l2_flushed": flushed_ms,
+    }
+
+    line = {
+        "metric": "Gcell-updates/s",
+        "value": value,
+        "unit": "Gcell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / max(1, accepted),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": "focused-beam 4096x2048 FP32 (plain method, full size)",
+            "nx": params.nx, "ny": params.ny, "cells": cells,
+            "variant": "exact (no FMA contraction; bit-identical to the oracle)" if exact else "fast (FMA)",
+            "cfl_target": params.cflwhish, "accepted": accepted, "rejected": int(st["rejected"]),
+            "T_end": st["T"],
+            "l2": "inputs larger than L2: each step reads one 100.7 MB state buffer and writes the "
+                  "other, 201 MB per step > 129 MB L2; launch_ms_l2_flushed is one step after "
+                  "writing 258 MB",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": accepted + int(st["rejected"]) + 1,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(params, seconds=args.cpu_seconds, max_steps=50)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fast", action="store_true", help="FMA-contracted variant instead of exact")
+    ap.add_argument("--e2e-steps", type=int, default=1000)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,589 @@
+// fv_api.cu -- the C ABI of include/fivonagi.h.
+//
+// Owns the device state of a simulation (two state buffers, the control
+// block, per-CTA CFL partials), runs the apps' initial-value hooks on the
+// host as the reference does, and drives the fused step kernel: bulk
+// attempts are replayed from a captured CUDA graph, the host synchronises
+// once per call, and every error comes back as an fv_status.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fv_internal.h"
+#include "fv_math.h"
+
+using namespace fvgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+fv_status fail(fv_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+#define FV_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(FV_CUDA_ERROR, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                  \
+  } while (0)
+
+// Graph of this many attempts, replayed for bulk runs.
+constexpr int kGraphAttempts = 32;
+constexpr int kMinRowsPerBlock = 32;
+
+__global__ void ctrl_begin_kernel(Ctrl *c, long long remaining, float t_stop) {
+  c->remaining = remaining;
+  c->t_stop = t_stop;
+  c->accepted = 0;
+  c->rejected = 0;
+  c->consecutive_rejects = 0;
+}
+
+__global__ void ctrl_reset_kernel(Ctrl *c, float dt, float T, int n) {
+  c->dt = dt;
+  c->T = T;
+  c->n = n;
+  c->cur = 0;
+  c->status = 0;
+  c->neg_flag = 0;
+  c->sim_error = 0;
+  c->consecutive_rejects = 0;
+  c->mdx = 0;
+  c->mdy = 0;
+  c->remaining = 0;
+  c->accepted = 0;
+  c->rejected = 0;
+  c->blocks_done = 0;
+  c->last_cfl = 0.0f;
+  c->t_stop = __int_as_float(0x7f800000);
+}
+
+__global__ void ctrl_scalars_kernel(Ctrl *c, float dt, float T, int n) {
+  c->dt = dt;
+  c->T = T;
+  c->n = n;
+}
+
+}  // namespace
+
+struct fv_handle {
+  fv_params params{};
+  DevParams dp{};
+  int device = 0;
+  size_t ncell = 0;
+  float *state_mem = nullptr;   // 2 buffers x 3 fields
+  size_t field_stride = 0;      // floats between fields (256-byte aligned)
+  float *dbg_mem = nullptr;
+  Ctrl *ctrl = nullptr;
+  Ctrl *ctrl_host = nullptr;    // pinned mirror for reads
+  float *partials = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  StepArgs args{};
+  int warps = 4;
+  bool exact = true;
+};
+
+namespace {
+
+int launch(fv_handle *h, int stage, const StepArgs &a) {
+  return h->exact ? launch_step_exact(a, h->warps, stage, h->stream)
+                  : launch_step_fast(a, h->warps, stage, h->stream);
+}
+
+fv_status validate(const fv_params *p) {
+  if (!p) return fail(FV_BAD_ARG, "params is NULL");
+  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM)
+    return fail(FV_BAD_ARG, "unknown app %d", p->app);
+  if (p->nx < 8 || p->ny < 8) return fail(FV_BAD_ARG, "grid %dx%d below 8x8", p->nx, p->ny);
+  if ((long long)p->nx * (long long)p->ny > (1LL << 30))
+    return fail(FV_BAD_ARG, "grid %dx%d above 2^30 cells", p->nx, p->ny);
+  if (!(p->xmax > 0) || !(p->ymax > 0)) return fail(FV_BAD_ARG, "xmax/ymax must be positive");
+  if (!(p->cflmax > 0) || !(p->cflwhish > 0) || !(p->dtini > 0))
+    return fail(FV_BAD_ARG, "cflmax, cflwhish and dtini must be positive");
+  if (p->moving_domain)
+    return fail(FV_BAD_ARG, "moving_domain is not supported by this build's step kernel");
+  if (p->app == FV_APP_FOCUSED_BEAM && !(p->ramp_periods > 0))
+    return fail(FV_BAD_ARG, "focused beam needs ramp_periods > 0");
+  return FV_OK;
+}
+
+DevParams make_dev_params(const fv_params &p) {
+  DevParams d{};
+  d.app = p.app;
+  d.nx = p.nx;
+  d.ny = p.ny;
+  d.cfl_even_only = p.cfl_even_only ? 1 : 0;
+  d.max_retries = p.max_retries > 0 ? p.max_retries : 64;
+  // FP32 rounding of each parameter, as `static const DATATYPEV` does
+  d.dx = float(p.xmax) / float(p.nx - 1);
+  d.dy = float(p.ymax) / float(p.ny - 1);
+  d.beta = float(p.beta);
+  d.diffdelta = float(p.diffdelta);
+  d.cflmax = float(p.cflmax);
+  d.cflwhish = float(p.cflwhish);
+  d.ampl = float(p.ampl);
+  d.frec = float(p.frec);
+  d.ispw = 2.0f * 3.1415926f * d.frec;  // Num2*PI*FREC, common/numbers.h:14
+  d.ispa = float(p.isp_a);
+  d.ispf = float(p.isp_f);
+  d.hifu_width = static_cast<int>(d.ispa / d.dy);
+  d.isprhoa = float(p.isp_rhoa);
+  d.ispc = float(p.isp_c);
+  d.mdt = float(p.mdt);
+  const float th = float(p.angle);
+  d.cos_th = fvm::cosf_(th);
+  d.sin_th = fvm::sinf_(th);
+  d.center = float(p.center);
+  d.halfap = float(p.aperture * 0.5);
+  d.ramp = p.ramp_periods > 0 ? float(p.frec / p.ramp_periods) : 0.0f;
+  return d;
+}
+
+// Host initial-value hooks (the reference's init<TTT> runs on the host too).
+void init_host(const fv_params &p, const DevParams &d, float *u1, float *u2, float *u3) {
+  const int nx = p.nx, ny = p.ny;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const size_t o = size_t(i) + size_t(j) * size_t(nx);
+      float v1 = 0.f, v2 = 0.f, v3 = 0.f;
+      if (p.app == FV_APP_TAYLOR_ANGLE_XY) {
+        // apps/taylor-angle-xy/init.h:19-27
+        const float th = float(p.angle);
+        const float c = fvm::cosf_(th), sn = fvm::sinf_(th);
+        const float rhop =
+            d.isprhoa * fvm::tanhf_(d.ispc * (float(i) * d.dx * c +
+                                              (float(j - ny / 2) * d.dy + d.mdt * sn) * sn +
+                                              float(p.tide)));
+        v1 = rhop;
+        v2 = rhop * c;
+        v3 = rhop * sn;
+      } else if (p.app == FV_APP_PLANE_WAVE) {
+        // sinusoidal plane wave in the taylor init form, in double
+        const double ddx = p.xmax / double(nx - 1), ddy = p.ymax / double(ny - 1);
+        const double ca = fvm::cos_d(p.angle), sa = fvm::sin_d(p.angle);
+        const double ph = 2.0 * 3.141592653589793 * p.frec * (double(i) * ddx * ca + double(j) * ddy * sa);
+        const double a = p.ampl * fvm::sin_d(ph);
+        v1 = float(a);
+        v2 = float(a * ca);
+        v3 = float(a * sa);
+      }
+      u1[o] = v1;
+      u2[o] = v2;
+      u3[o] = v3;
+    }
+}
+
+float *field_ptr(fv_handle *h, int buf, int f) {
+  return h->state_mem + (size_t(buf) * 3 + size_t(f)) * h->field_stride;
+}
+
+fv_status read_ctrl(fv_handle *h) {
+  FV_CUDA(cudaMemcpyAsync(h->ctrl_host, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+void fill_stats(const fv_handle *h, fv_run_stats *st) {
+  if (!st) return;
+  const Ctrl &c = *h->ctrl_host;
+  st->accepted = c.accepted;
+  st->rejected = c.rejected;
+  st->dt = c.dt;
+  st->T = c.T;
+  st->cfl = c.last_cfl;
+  st->n = c.n;
+  st->status = c.status;
+  st->mdx = c.mdx;
+  st->mdy = c.mdy;
+}
+
+fv_status ensure_graph(fv_handle *h) {
+  if (h->graph) return FV_OK;
+  cudaGraph_t g = nullptr;
+  FV_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  for (int k = 0; k < kGraphAttempts && rc == 0; ++k) rc = launch(h, -1, h->args);
+  cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+  if (rc != 0) return fail(FV_CUDA_ERROR, "step launch during capture: %s", cudaGetErrorString((cudaError_t)rc));
+  if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
+  ec = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ec != cudaSuccess) {
+    h->graph = nullptr;
+    return fail(FV_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ec));
+  }
+  return FV_OK;
+}
+
+// Enqueue n attempts: whole graphs, then single launches.
+fv_status enqueue_attempts(fv_handle *h, long long n) {
+  if (n >= kGraphAttempts) {
+    fv_status s = ensure_graph(h);
+    if (s != FV_OK) return s;
+    while (n >= kGraphAttempts) {
+      FV_CUDA(cudaGraphLaunch(h->graph, h->stream));
+      n -= kGraphAttempts;
+    }
+  }
+  for (long long k = 0; k < n; ++k) {
+    int rc = launch(h, -1, h->args);
+    if (rc != 0) return fail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
+  }
+  return FV_OK;
+}
+
+fv_status reset_ctrl(fv_handle *h) {
+  const DevParams &d = h->dp;
+  ctrl_reset_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, float(h->params.dtini),
+                                            -float(h->params.tide), 0);
+  (void)d;
+  FV_CUDA(cudaGetLastError());
+  return FV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fv_version(void) { return "fivonagi-gb300 1 (sm_103a)"; }
+
+const char *fv_last_error_string(void) { return g_last_error.c_str(); }
+
+fv_status fv_default_params(int32_t app, fv_params *out) {
+  if (!out) return fail(FV_BAD_ARG, "out is NULL");
+  fv_params p;
+  std::memset(&p, 0, sizeof(p));
+  p.app = app;
+  p.cfl_even_only = 1;
+  p.exact = 1;
+  p.max_retries = 64;
+  p.cflmax = 1.0;
+  p.cflwhish = double(float(90 / 100.0));  // CFLWHISH = CFLW/100.0 with CFLW = 90
+  p.dtini = double(0.005f);
+  switch (app) {
+    case FV_APP_HIFU_BEAM: {
+      // apps/hifu-beam/parameters.h:12-104 with ETAC=1, CFLW=90, ISPAM=30;
+      // each value is the FP32 result of the reference's own expression.
+      const int NX = 512, NY = 1024;
+      const float XMAX = 12.5f * 2.0f, YMAX = 12.5f * 4.0f, FREC = 1.0f;
+      const float PI = 3.1415926f;
+      const float ISPW = 2.0f * PI * FREC;
+      const float ISPlambda = 2.0f * PI / ISPW;
+      const float ISPa = 30 * ISPlambda;
+      const float ISPF = float(50.0 * ISPlambda / (XMAX / (NX - 1)));
+      const float TIDE = float(std::floor(2 + 4 / FREC +
+                                          (ISPa * ISPa * (XMAX / (NX - 1))) /
+                                              (2.0 * ISPF * (YMAX / (NY - 1)) * (YMAX / (NY - 1)))));
+      p.nx = NX;
+      p.ny = NY;
+      p.xmax = XMAX;
+      p.ymax = YMAX;
+      p.beta = double(4.8f);
+      p.diffdelta = double(0.0002974f);
+      p.ampl = double(0.0004217f);
+      p.frec = FREC;
+      p.isp_a = ISPa;
+      p.isp_f = ISPF;
+      p.tide = TIDE;
+      p.mdvx = 1.0;
+      p.mdvy = 0.0;
+      p.mdt = double(XMAX * 0.5f);
+      p.moving_domain = 1;
+      break;
+    }
+    case FV_APP_TAYLOR_ANGLE_XY: {
+      // apps/taylor-angle-xy/parameters.h:12-109 with ETAC=1, CFLW=90,
+      // ANGLE=0, SIN=0, COS=1
+      const float XMAX = 12.5f, YMAX = 12.5f, BETA = 1.0f, DIFFDELTA = 0.0000001f;
+      const int COS = 1, SIN = 0;
+      const float MDT = float(XMAX * 0.5 / COS);
+      p.nx = 64;
+      p.ny = 64;
+      p.xmax = XMAX;
+      p.ymax = YMAX;
+      p.beta = BETA;
+      p.diffdelta = DIFFDELTA;
+      p.frec = 1.0;
+      p.mdvx = COS;
+      p.mdvy = SIN;
+      p.mdt = MDT;
+      p.tide = float(std::ceil(4 + (YMAX * 0.5 - MDT * SIN) * SIN));
+      p.isp_rhoa = double(-DIFFDELTA / BETA);
+      p.isp_c = double(2.1972245773362196f);
+      p.angle = 0.0;
+      p.ampl = -p.isp_rhoa;
+      p.moving_domain = 1;
+      break;
+    }
+    case FV_APP_PLANE_WAVE: {
+      // 512 x 512, 16 cells per wavelength, 30 degrees, Mach 1e-3
+      p.nx = 512;
+      p.ny = 512;
+      p.xmax = 511.0 / 16.0;
+      p.ymax = 511.0 / 16.0;
+      p.beta = 3.5;
+      p.diffdelta = 1e-4;
+      p.ampl = 1e-3;
+      p.frec = 1.0;
+      p.angle = 3.141592653589793 / 6.0;
+      p.tide = 0.0;
+      break;
+    }
+    case FV_APP_FOCUSED_BEAM: {
+      // 4096 (axial) x 2048 (lateral), 24 cells per wavelength, aperture
+      // 1024 cells centred on j = 1024, focus 3000 cells, Mach 5e-3
+      // reached over 5 periods
+      p.nx = 4096;
+      p.ny = 2048;
+      p.xmax = 4095.0 / 24.0;
+      p.ymax = 2047.0 / 24.0;
+      p.beta = 3.5;
+      p.diffdelta = 5e-5;
+      p.ampl = 5e-3;
+      p.frec = 1.0;
+      p.isp_f = 3000.0;
+      p.aperture = 1024.0;
+      p.center = 1024.0;
+      p.ramp_periods = 5.0;
+      p.tide = 0.0;
+      break;
+    }
+    default:
+      return fail(FV_BAD_ARG, "unknown app %d", app);
+  }
+  *out = p;
+  return FV_OK;
+}
+
+fv_status fv_create(const fv_params *p, fv_handle **out) {
+  if (!out) return fail(FV_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  fv_status s = validate(p);
+  if (s != FV_OK) return s;
+  int dev = 0, ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(FV_NO_DEVICE, "no CUDA device");
+  FV_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  FV_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(FV_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a", dev,
+                prop.major, prop.minor);
+
+  fv_handle *h = new (std::nothrow) fv_handle();
+  if (!h) return fail(FV_CUDA_ERROR, "out of host memory");
+  h->params = *p;
+  h->dp = make_dev_params(*p);
+  h->device = dev;
+  h->exact = p->exact != 0;
+  h->ncell = size_t(p->nx) * size_t(p->ny);
+  h->field_stride = (h->ncell + 63) & ~size_t(63);
+  auto cleanup = [&](fv_status st) {
+    fv_destroy(h);
+    return st;
+  };
+  cudaError_t e = cudaMalloc(&h->state_mem, 6 * h->field_stride * sizeof(float));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc state: %s", cudaGetErrorString(e)));
+  e = cudaMalloc(&h->ctrl, sizeof(Ctrl));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc ctrl: %s", cudaGetErrorString(e)));
+  e = cudaMallocHost(&h->ctrl_host, sizeof(Ctrl));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMallocHost: %s", cudaGetErrorString(e)));
+  e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "stream: %s", cudaGetErrorString(e)));
+  h->stream = h->own_stream;
+
+  // launch shape: persistent CTAs, each streaming a balanced share of the
+  // (strip, row) space
+  const int strip_cols = h->warps * kWarpCols;
+  const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
+  const long long work = (long long)nstrips * p->ny;
+  const int per_sm = h->exact ? max_blocks_per_sm_exact(h->warps, -1) : max_blocks_per_sm_fast(h->warps, -1);
+  long long blocks = (long long)per_sm * prop.multiProcessorCount;
+  blocks = std::min(blocks, std::max(1LL, work / kMinRowsPerBlock));
+  e = cudaMalloc(&h->partials, size_t(blocks) * sizeof(float));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc partials: %s", cudaGetErrorString(e)));
+
+  StepArgs &a = h->args;
+  a.p = h->dp;
+  for (int b = 0; b < 2; ++b)
+    for (int f = 0; f < 3; ++f) a.state[b][f] = field_ptr(h, b, f);
+  a.ctrl = h->ctrl;
+  a.partials = h->partials;
+  a.nstrips = nstrips;
+  a.nblocks = int(blocks);
+  a.work = work;
+  FV_CUDA(cudaMemsetAsync(h->state_mem, 0, 6 * h->field_stride * sizeof(float), h->stream));
+  s = reset_ctrl(h);
+  if (s != FV_OK) return cleanup(s);
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "create sync: %s", cudaGetErrorString(e)));
+  *out = h;
+  return FV_OK;
+}
+
+fv_status fv_destroy(fv_handle *h) {
+  if (!h) return FV_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->state_mem) cudaFree(h->state_mem);
+  if (h->dbg_mem) cudaFree(h->dbg_mem);
+  if (h->ctrl) cudaFree(h->ctrl);
+  if (h->ctrl_host) cudaFreeHost(h->ctrl_host);
+  if (h->partials) cudaFree(h->partials);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return FV_OK;
+}
+
+fv_status fv_set_stream(fv_handle *h, void *cuda_stream) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+  return FV_OK;
+}
+
+fv_status fv_init_state(fv_handle *h) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  std::vector<float> u(3 * h->ncell);
+  init_host(h->params, h->dp, u.data(), u.data() + h->ncell, u.data() + 2 * h->ncell);
+  return fv_set_state(h, u.data(), u.data() + h->ncell, u.data() + 2 * h->ncell, 0);
+}
+
+fv_status fv_set_state(fv_handle *h, const float *u1, const float *u2, const float *u3,
+                       int32_t on_device) {
+  if (!h || !u1 || !u2 || !u3) return fail(FV_BAD_ARG, "NULL argument");
+  const float *src[3] = {u1, u2, u3};
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  for (int f = 0; f < 3; ++f)
+    FV_CUDA(cudaMemcpyAsync(field_ptr(h, 0, f), src[f], h->ncell * sizeof(float), kind, h->stream));
+  fv_status s = reset_ctrl(h);
+  if (s != FV_OK) return s;
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+fv_status fv_get_state(fv_handle *h, float *u1, float *u2, float *u3, int32_t on_device) {
+  if (!h || !u1 || !u2 || !u3) return fail(FV_BAD_ARG, "NULL argument");
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  const int cur = h->ctrl_host->cur;
+  float *dst[3] = {u1, u2, u3};
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  for (int f = 0; f < 3; ++f)
+    FV_CUDA(cudaMemcpyAsync(dst[f], field_ptr(h, cur, f), h->ncell * sizeof(float), kind, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+fv_status fv_set_scalars(fv_handle *h, double dt, double T, int32_t n) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  ctrl_scalars_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, float(dt), float(T), n);
+  FV_CUDA(cudaGetLastError());
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+fv_status fv_get_stats(fv_handle *h, fv_run_stats *out) {
+  if (!h || !out) return fail(FV_BAD_ARG, "NULL argument");
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  fill_stats(h, out);
+  return FV_OK;
+}
+
+fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts) {
+  if (!h || nattempts < 0) return fail(FV_BAD_ARG, "bad argument");
+  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nattempts,
+                                            std::numeric_limits<float>::infinity());
+  FV_CUDA(cudaGetLastError());
+  return enqueue_attempts(h, nattempts);
+}
+
+fv_status fv_sync(fv_handle *h, fv_run_stats *out) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  fill_stats(h, out);
+  return h->ctrl_host->status ? (fv_status)h->ctrl_host->status : FV_OK;
+}
+
+fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
+  if (!h || nsteps < 0) return fail(FV_BAD_ARG, "bad argument");
+  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nsteps,
+                                            std::numeric_limits<float>::infinity());
+  FV_CUDA(cudaGetLastError());
+  long long todo = nsteps;
+  for (;;) {
+    fv_status s = enqueue_attempts(h, todo);
+    if (s != FV_OK) return s;
+    s = read_ctrl(h);
+    if (s != FV_OK) return s;
+    const Ctrl &c = *h->ctrl_host;
+    if (c.status != 0 || c.remaining <= 0) break;
+    todo = c.remaining;  // rejected attempts are made up
+  }
+  fill_stats(h, out);
+  const int st = h->ctrl_host->status;
+  if (st == FV_NEGATIVE_EIGENVALUE) return fail(FV_NEGATIVE_EIGENVALUE, "negative eigenvalue (tmp3 < 0)");
+  if (st == FV_DT_TOO_LARGE) return fail(FV_DT_TOO_LARGE, "dt too large after %d retries", h->dp.max_retries);
+  return st ? (fv_status)st : FV_OK;
+}
+
+fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, std::numeric_limits<long long>::max(),
+                                            float(t_stop));
+  FV_CUDA(cudaGetLastError());
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  while (h->ctrl_host->status == 0 && h->ctrl_host->T < float(t_stop)) {
+    const double dt = std::max(double(h->ctrl_host->dt), 1e-30);
+    long long est = (long long)std::ceil((double(t_stop) - h->ctrl_host->T) / dt) + 1;
+    est = std::min<long long>(std::max<long long>(est, 1), 1 << 16);
+    s = enqueue_attempts(h, est);
+    if (s != FV_OK) return s;
+    s = read_ctrl(h);
+    if (s != FV_OK) return s;
+  }
+  fill_stats(h, out);
+  const int st = h->ctrl_host->status;
+  if (st) return fail((fv_status)st, "device run stopped with status %d", st);
+  return FV_OK;
+}
+
+fv_status fv_debug_step(fv_handle *h, int32_t stage, float *u1, float *u2, float *u3) {
+  if (!h || !u1 || !u2 || !u3) return fail(FV_BAD_ARG, "NULL argument");
+  if (stage < FV_STAGE_BOUNDARY || stage > FV_STAGE_SOURCE) return fail(FV_BAD_ARG, "bad stage %d", stage);
+  if (!h->dbg_mem) FV_CUDA(cudaMalloc(&h->dbg_mem, 3 * h->field_stride * sizeof(float)));
+  StepArgs a = h->args;
+  for (int f = 0; f < 3; ++f) a.dbg[f] = h->dbg_mem + size_t(f) * h->field_stride;
+  FV_CUDA(cudaMemsetAsync(h->dbg_mem, 0, 3 * h->field_stride * sizeof(float), h->stream));
+  int rc = launch(h, stage, a);
+  if (rc != 0) return fail(FV_CUDA_ERROR, "stage launch: %s", cudaGetErrorString((cudaError_t)rc));
+  float *dst[3] = {u1, u2, u3};
+  for (int f = 0; f < 3; ++f)
+    FV_CUDA(cudaMemcpyAsync(dst[f], a.dbg[f], h->ncell * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+}  // extern "C"

@@ -15,7 +15,7 @@
 namespace fvo {
 
 template <class R>
-Sim<R>::Sim(const fv_params &pp) : p(pp) {
+Sim<R>::Sim(const fv_params &pp, bool fvm_math) : p(pp), fvm_mode(fvm_math) {
   nx = p.nx;
   ny = p.ny;
   // dx = XMAX/(NX-1), dy = YMAX/(NY-1) in working precision
@@ -67,26 +67,29 @@ template <class R> void Sim<R>::init_state() {
       if (app == FV_APP_TAYLOR_ANGLE_XY) {
         // apps/taylor-angle-xy/init.h:19-27
         const R th = ac.isptheta;
+        const bool m = fvm_mode;
         R rhop = ac.isprhoa *
-                 std::tanh(ac.ispc * (R(i) * dx * std::cos(th) +
-                                      (R(j - ny / 2) * dy + ac.mdt * std::sin(th)) *
-                                          std::sin(th) +
-                                      R(p.tide)));
+                 Fn<R>::tanh(ac.ispc * (R(i) * dx * Fn<R>::cos(th, m) +
+                                        (R(j - ny / 2) * dy + ac.mdt * Fn<R>::sin(th, m)) *
+                                            Fn<R>::sin(th, m) +
+                                        R(p.tide)),
+                             m);
         v1 = rhop;
-        v2 = rhop * std::cos(th);
-        v3 = rhop * std::sin(th);
+        v2 = rhop * Fn<R>::cos(th, m);
+        v3 = rhop * Fn<R>::sin(th, m);
       } else if (app == FV_APP_PLANE_WAVE) {
         // u1 = A sin(2 pi FREC (x cos a + y sin a)), u2,u3 = u1 (cos a, sin a):
         // the taylor init form (init.h:25-27) with a sinusoidal profile,
         // evaluated in double and rounded once.
         const double ddx = p.xmax / double(nx - 1), ddy = p.ymax / double(ny - 1);
+        const bool m = fvm_mode;
+        const double ca = Fn<double>::cos(p.angle, m), sa = Fn<double>::sin(p.angle, m);
         const double ph = 2.0 * 3.141592653589793 * p.frec *
-                          (double(i) * ddx * std::cos(p.angle) +
-                           double(j) * ddy * std::sin(p.angle));
-        const double a = p.ampl * std::sin(ph);
+                          (double(i) * ddx * ca + double(j) * ddy * sa);
+        const double a = p.ampl * Fn<double>::sin(ph, m);
         v1 = R(a);
-        v2 = R(a * std::cos(p.angle));
-        v3 = R(a * std::sin(p.angle));
+        v2 = R(a * ca);
+        v3 = R(a * sa);
       }
       // hifu-beam (apps/hifu-beam/init.h:16-25) and the focused beam: zeros
       u[0][o] = v1;
@@ -101,10 +104,11 @@ template <class R> void Sim<R>::init_state() {
 
 // packet() of apps/hifu-beam/boundary.h:10-17. opT is evaluated in double
 // (the literals 2.0 and 8.0 are double) and rounded to R on assignment.
-template <class R> static inline R hifu_packet(const AppConsts<R> &ac, R T, R phi) {
+template <class R>
+static inline R hifu_packet(const AppConsts<R> &ac, R T, R phi, bool m) {
   R opT = R(2.0 * double(ac.frec) * double(T + phi) / 8.0);
-  R res = ac.ampl * std::sin(ac.ispw * (T + phi));
-  res = res * std::exp(-opT * opT * opT * opT * opT * opT * opT * opT * opT * opT);
+  R res = ac.ampl * Fn<R>::sin(ac.ispw * (T + phi), m);
+  res = res * Fn<R>::exp(-opT * opT * opT * opT * opT * opT * opT * opT * opT * opT, m);
   return res;
 }
 
@@ -128,14 +132,16 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
           // apps/taylor-angle-xy/boundary.h:38-55: every ghost cell, corners
           // included, is the analytic profile.
           const R th = ac.isptheta;
+          const bool m = fvm_mode;
           R rhop = ac.isprhoa *
-                   std::tanh(ac.ispc * (R(i + mdx) * dx * std::cos(th) +
-                                        (R(j + mdy - ny / 2) * dy + ac.mdt * std::sin(th)) *
-                                            std::sin(th) -
-                                        T));
+                   Fn<R>::tanh(ac.ispc * (R(i + mdx) * dx * Fn<R>::cos(th, m) +
+                                          (R(j + mdy - ny / 2) * dy + ac.mdt * Fn<R>::sin(th, m)) *
+                                              Fn<R>::sin(th, m) -
+                                          T),
+                               m);
           v1 = rhop;
-          v2 = rhop * std::cos(th);
-          v3 = rhop * std::sin(th);
+          v2 = rhop * Fn<R>::cos(th, m);
+          v3 = rhop * Fn<R>::sin(th, m);
         } else if (corner) {
           // apps/hifu-beam/boundary.h:125-133 (and the same convention for
           // the plane-wave and focused-beam apps)
@@ -160,7 +166,7 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
               R nux = ac.ispf / nudenom;
               R nuy = -static_cast<R>(jprime) / nudenom;
               R phi = (dx * jprime2) / (R(2) * ac.ispf);
-              R pack = hifu_packet(ac, T, phi);
+              R pack = hifu_packet(ac, T, phi, fvm_mode);
               v1 = pack;
               v2 = nux * pack * (pack + one);
               v3 = nuy * pack * (pack + one);
@@ -177,7 +183,7 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
               R phi = (dx * jp2) / (R(2) * ac.ispf);
               R t = T + phi;
               R ramp = getmin(getmax(t * ac.ramp, zero), one);
-              R pack = ac.ampl * ramp * std::sin(ac.ispw * t);
+              R pack = ac.ampl * ramp * Fn<R>::sin(ac.ispw * t, fvm_mode);
               v1 = pack;
               v2 = nux * pack * (pack + one);
               v3 = nuy * pack * (pack + one);
@@ -440,12 +446,15 @@ template <class R> void stats_of(const fvo::Sim<R> &s, fv_run_stats *st) {
 
 extern "C" {
 
-void *fvo_create(const fv_params *p, int prec) {
+// flags bit 0: evaluate the apps' transcendental functions with fv_math.h
+// (see Fn<R>) instead of the host libm.
+void *fvo_create(const fv_params *p, int prec, int flags) {
   if (!p || (prec != 4 && prec != 8) || p->nx < 8 || p->ny < 8) return nullptr;
   Handle *h = new Handle();
   h->prec = prec;
-  if (prec == 4) h->f = new fvo::Sim<float>(*p);
-  else h->d = new fvo::Sim<double>(*p);
+  const bool m = (flags & 1) != 0;
+  if (prec == 4) h->f = new fvo::Sim<float>(*p, m);
+  else h->d = new fvo::Sim<double>(*p, m);
   return h;
 }
 
@@ -538,6 +547,19 @@ int fvo_debug_step(void *hv, int stage, void *u1, void *u2, void *u3) {
     s.accepted = acc; s.rejected = rej; s.status = st; s.mdx = mx; s.mdy = my;
   });
   return rc == 2 ? FV_NEGATIVE_EIGENVALUE : FV_OK;
+}
+
+// fv_math.h (fn 0 sin, 1 cos, 2 exp, 3 tanh) evaluated on the host over n
+// floats, for checking those functions against the host libm.
+void fvo_fvm_eval(int fn, const float *x, float *y, int64_t n) {
+  for (int64_t k = 0; k < n; ++k) {
+    switch (fn) {
+      case 0: y[k] = fvm::sinf_(x[k]); break;
+      case 1: y[k] = fvm::cosf_(x[k]); break;
+      case 2: y[k] = fvm::expf_(x[k]); break;
+      default: y[k] = fvm::tanhf_(x[k]); break;
+    }
+  }
 }
 
 // The CFL of the step that fvo_debug_step or fvo_run attempted last.

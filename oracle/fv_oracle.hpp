@@ -30,8 +30,29 @@
 #include <vector>
 
 #include "../include/fivonagi.h"
+#include "../fivonagi_gb300/csrc/fv_math.h"
 
 namespace fvo {
+
+// The apps' transcendental functions. libm mode calls the host libm, as the
+// reference's hooks do when built for the host (oracle/ref_shim.cpp), and
+// is the mode pinned to the reference. fvm mode evaluates them with
+// fv_math.h, the portable functions the library uses on both host and
+// device, so that the restatement and the CUDA path can be compared bit for
+// bit; the two modes differ only in those function values.
+template <class R> struct Fn;
+template <> struct Fn<float> {
+  static float sin(float x, bool m) { return m ? fvm::sinf_(x) : std::sin(x); }
+  static float cos(float x, bool m) { return m ? fvm::cosf_(x) : std::cos(x); }
+  static float exp(float x, bool m) { return m ? fvm::expf_(x) : std::exp(x); }
+  static float tanh(float x, bool m) { return m ? fvm::tanhf_(x) : std::tanh(x); }
+};
+template <> struct Fn<double> {
+  static double sin(double x, bool m) { return m ? fvm::sin_d(x) : std::sin(x); }
+  static double cos(double x, bool m) { return m ? fvm::cos_d(x) : std::cos(x); }
+  static double exp(double x, bool m) { return m ? fvm::exp_d(x) : std::exp(x); }
+  static double tanh(double x, bool m) { return m ? fvm::tanh_d(x) : std::tanh(x); }
+};
 
 // getmax / getmin exactly as common/main.cu:63-69: the second argument wins
 // ties and NaN comparisons.
@@ -176,6 +197,7 @@ template <class R> struct AppConsts {
 template <class R> class Sim {
  public:
   fv_params p{};
+  bool fvm_mode = false;  // see Fn<R>
   int nx = 0, ny = 0;
   R dx{}, dy{}, beta{}, diffdelta{}, cflmax{}, cflwhish{};
   AppConsts<R> ac{};
@@ -193,7 +215,7 @@ template <class R> class Sim {
   std::vector<Wave<R>> wv;  // waves of one sweep, indexed by cell offset
   std::vector<R> fadd[3];
 
-  explicit Sim(const fv_params &pp);
+  explicit Sim(const fv_params &pp, bool fvm_math = false);
   size_t size() const { return size_t(nx) * size_t(ny); }
   size_t off(int i, int j) const { return size_t(i) + size_t(j) * size_t(nx); }
   bool interior(int i, int j) const {

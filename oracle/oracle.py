@@ -47,7 +47,7 @@ def _load_oracle() -> C.CDLL:
         lib = C.CDLL(ORACLE_LIB)
         P = C.c_void_p
         lib.fvo_create.restype = P
-        lib.fvo_create.argtypes = [C.POINTER(FvParams), C.c_int]
+        lib.fvo_create.argtypes = [C.POINTER(FvParams), C.c_int, C.c_int]
         lib.fvo_destroy.argtypes = [P]
         lib.fvo_set_threads.restype = C.c_int
         lib.fvo_set_threads.argtypes = [C.c_int]
@@ -61,6 +61,7 @@ def _load_oracle() -> C.CDLL:
         lib.fvo_debug_step.argtypes = [P, C.c_int, P, P, P]
         lib.fvo_last_cfl.restype = C.c_double
         lib.fvo_last_cfl.argtypes = [P]
+        lib.fvo_fvm_eval.argtypes = [C.c_int, P, P, C.c_int64]
         _oracle = lib
     return _oracle
 
@@ -78,6 +79,15 @@ def _load_ref() -> C.CDLL:
     return _ref
 
 
+def fvm_eval(fn: str, x) -> np.ndarray:
+    """fv_math.h's float function `fn` (sin, cos, exp, tanh) on the host."""
+    code = {"sin": 0, "cos": 1, "exp": 2, "tanh": 3}[fn]
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    _load_oracle().fvo_fvm_eval(code, _ptr(x), _ptr(y), x.size)
+    return y
+
+
 def set_threads(n: int) -> int:
     return _load_oracle().fvo_set_threads(int(n))
 
@@ -87,14 +97,22 @@ def _ptr(a: np.ndarray) -> int:
 
 
 class OracleSim:
-    """One simulation of the CPU restatement, mirroring the C ABI's handle."""
+    """One simulation of the CPU restatement, mirroring the C ABI's handle.
 
-    def __init__(self, params: FvParams, dtype=np.float32):
+    math="libm": the apps' sin/exp/tanh from the host libm (the mode pinned
+    to the reference build); math="fvm": from fv_math.h, as the library
+    evaluates them (the mode the CUDA path is compared with bit for bit).
+    """
+
+    def __init__(self, params: FvParams, dtype=np.float32, math: str = "libm"):
+        if math not in ("libm", "fvm"):
+            raise ValueError("math must be 'libm' or 'fvm'")
         self.lib = _load_oracle()
         self.params = params.copy()
         self.dtype = np.dtype(dtype)
+        self.math = math
         prec = self.dtype.itemsize
-        self.h = self.lib.fvo_create(C.byref(self.params), prec)
+        self.h = self.lib.fvo_create(C.byref(self.params), prec, 1 if math == "fvm" else 0)
         if not self.h:
             raise ValueError("oracle rejected the parameters")
         self.shape = (params.ny, params.nx)
