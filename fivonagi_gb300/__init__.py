@@ -8,11 +8,11 @@ from ._abi import (APP_NAMES, FV_APP_FOCUSED_BEAM, FV_APP_HIFU_BEAM, FV_APP_PLAN
                    FV_APP_TAYLOR_ANGLE_XY, FV_STAGE_BOUNDARY, FV_STAGE_SOURCE,
                    FV_STAGE_SWEEP_X, FV_STAGE_SWEEP_Y, FvError, FvParams, FvRunStats,
                    default_params, load_library)
-from .solver import Simulation
+from .solver import Batch, Simulation
 
 __all__ = [
     "APP_NAMES", "FV_APP_FOCUSED_BEAM", "FV_APP_HIFU_BEAM", "FV_APP_PLANE_WAVE",
     "FV_APP_TAYLOR_ANGLE_XY", "FV_STAGE_BOUNDARY", "FV_STAGE_SOURCE", "FV_STAGE_SWEEP_X",
-    "FV_STAGE_SWEEP_Y", "FvError", "FvParams", "FvRunStats", "Simulation", "default_params",
+    "FV_STAGE_SWEEP_Y", "Batch", "FvError", "FvParams", "FvRunStats", "Simulation", "default_params",
     "load_library",
 ]

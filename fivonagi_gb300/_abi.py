@@ -143,6 +143,19 @@ PROTOTYPES = {
     "fv_launch_attempts": (C.c_int, [_P, C.c_int64]),
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
+    "fv_set_launch": (C.c_int, [_P, C.c_int32]),
+    "fv_get_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "fv_batch_create": (C.c_int, [C.c_int32, C.POINTER(FvParams), C.POINTER(_P)]),
+    "fv_batch_destroy": (C.c_int, [_P]),
+    "fv_batch_set_stream": (C.c_int, [_P, _P]),
+    "fv_batch_init_state": (C.c_int, [_P]),
+    "fv_batch_set_state": (C.c_int, [_P, C.c_int32, _P, _P, _P, C.c_int32]),
+    "fv_batch_get_state": (C.c_int, [_P, C.c_int32, _P, _P, _P, C.c_int32]),
+    "fv_batch_run": (C.c_int, [_P, C.c_int64, C.POINTER(FvRunStats)]),
+    "fv_batch_launch_attempts": (C.c_int, [_P, C.c_int64]),
+    "fv_batch_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_batch_set_launch": (C.c_int, [_P, C.c_int32]),
+    "fv_batch_get_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -1,0 +1,90 @@
+"""Launch-shape autotuner for the step kernel.
+
+The step kernel's only free launch parameter is the number of persistent
+CTAs that share the grid's (column strip, row) work (fv_set_launch). More
+waves keep every SM full to the end, but shorter row segments repeat the
+8-row warm-up/drain of the streaming loop, so the best count depends on the
+grid size. `tune` times a few candidates, in waves of the CTAs resident at
+once, on a scratch copy of the simulation, and caches the winner per
+(device, grid, variant) in a JSON file next to the library.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+from . import _abi
+from ._abi import FvParams
+
+CACHE = os.path.join(_abi.LIB_DIR, "autotune.json")
+WAVES = (1, 2, 3, 4, 6, 8)
+
+
+def _key(params: FvParams, device: str) -> str:
+    return f"{device}|{params.nx}x{params.ny}|exact={params.exact}"
+
+
+def _load() -> dict:
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(d: dict) -> None:
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    tmp = CACHE + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(d, f, indent=1, sort_keys=True)
+    os.replace(tmp, CACHE)
+
+
+def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> int:
+    """Best CTA count for `params` on the current device (cached)."""
+    import torch
+
+    from .solver import Simulation
+
+    device = torch.cuda.get_device_name()
+    key = _key(params, device)
+    cache = _load()
+    if key in cache and not refresh:
+        return int(cache[key]["blocks"])
+    sim = Simulation(params)
+    try:
+        sim.init_state()
+        stream = torch.cuda.Stream()
+        sim.set_stream(stream.cuda_stream)
+        sim.run(10)
+        _, resident = sim.get_launch()
+        results = {}
+        for w in WAVES:
+            b = w * resident
+            try:
+                sim.set_launch(b)
+            except _abi.FvError:
+                continue
+            sim.run(4)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.launch_attempts(steps)
+            e1.record(stream)
+            stream.synchronize()
+            sim.sync()
+            results[b] = e0.elapsed_time(e1) / steps
+        best = min(results, key=results.get)
+    finally:
+        sim.close()
+    cache[key] = {"blocks": best, "ms_per_step": results[best],
+                  "candidates": {str(k): v for k, v in sorted(results.items())}}
+    _store(cache)
+    return best
+
+
+def apply(sim, refresh: bool = False) -> int:
+    """Tune for `sim`'s parameters and set its launch shape; returns the CTAs."""
+    b = tune(sim.params, refresh=refresh)
+    sim.set_launch(b)
+    return b

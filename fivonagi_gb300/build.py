@@ -1,9 +1,10 @@
 """Build libfivonagi.so in-tree with nvcc for sm_103a.
 
-Three translation units, compiled in parallel:
+Translation units, compiled in parallel:
   fv_step.cu (exact)  --fmad=false: no FMA contraction, bit-identical to the oracle
   fv_step.cu (fast)   --fmad=true : contracted FMAs, checked against the FP32 tolerance
-  fv_api.cu           the C ABI (host code, small kernels for the control block)
+  fv_api.cu           the C ABI of one simulation (host code, control-block kernels)
+  fv_batch.cu         the C ABI of batches
 """
 from __future__ import annotations
 
@@ -33,11 +34,11 @@ def nvcc() -> str:
 
 def _units():
     step = os.path.join(CSRC, "fv_step.cu")
-    api = os.path.join(CSRC, "fv_api.cu")
     return [
         ("fv_step_exact.o", step, ["-DFV_VARIANT_EXACT=1", "--fmad=false"]),
         ("fv_step_fast.o", step, ["-DFV_VARIANT_EXACT=0", "--fmad=true"]),
-        ("fv_api.o", api, []),
+        ("fv_api.o", os.path.join(CSRC, "fv_api.cu"), []),
+        ("fv_batch.o", os.path.join(CSRC, "fv_batch.cu"), []),
     ]
 
 

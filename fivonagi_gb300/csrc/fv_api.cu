@@ -83,6 +83,10 @@ __global__ void ctrl_scalars_kernel(Ctrl *c, float dt, float T, int n) {
 
 }  // namespace
 
+namespace fvgb {
+void set_last_error(const char *msg) { g_last_error = msg; }
+}  // namespace fvgb
+
 struct fv_handle {
   fv_params params{};
   DevParams dp{};
@@ -91,6 +95,7 @@ struct fv_handle {
   float *state_mem = nullptr;   // 2 buffers x 3 fields
   size_t field_stride = 0;      // floats between fields (256-byte aligned)
   float *dbg_mem = nullptr;
+  float *frame_mem = nullptr;   // ghost frame, 3 fields
   Ctrl *ctrl = nullptr;
   Ctrl *ctrl_host = nullptr;    // pinned mirror for reads
   float *partials = nullptr;
@@ -100,6 +105,8 @@ struct fv_handle {
   StepArgs args{};
   int warps = 4;
   bool exact = true;
+  int max_resident = 0;       // CTAs that fit on the device at once
+  int partials_cap = 0;       // capacity of `partials`
 };
 
 namespace {
@@ -119,8 +126,8 @@ fv_status validate(const fv_params *p) {
   if (!(p->xmax > 0) || !(p->ymax > 0)) return fail(FV_BAD_ARG, "xmax/ymax must be positive");
   if (!(p->cflmax > 0) || !(p->cflwhish > 0) || !(p->dtini > 0))
     return fail(FV_BAD_ARG, "cflmax, cflwhish and dtini must be positive");
-  if (p->moving_domain)
-    return fail(FV_BAD_ARG, "moving_domain is not supported by this build's step kernel");
+  if (p->moving_domain && (p->mdvx < 0 || p->mdvy < 0))
+    return fail(FV_BAD_ARG, "moving_domain needs mdvx, mdvy >= 0");
   if (p->app == FV_APP_FOCUSED_BEAM && !(p->ramp_periods > 0))
     return fail(FV_BAD_ARG, "focused beam needs ramp_periods > 0");
   return FV_OK;
@@ -133,6 +140,9 @@ DevParams make_dev_params(const fv_params &p) {
   d.ny = p.ny;
   d.cfl_even_only = p.cfl_even_only ? 1 : 0;
   d.max_retries = p.max_retries > 0 ? p.max_retries : 64;
+  d.moving_domain = p.moving_domain ? 1 : 0;
+  d.mdvx = float(p.mdvx);
+  d.mdvy = float(p.mdvy);
   // FP32 rounding of each parameter, as `static const DATATYPEV` does
   d.dx = float(p.xmax) / float(p.nx - 1);
   d.dy = float(p.ymax) / float(p.ny - 1);
@@ -192,6 +202,19 @@ void init_host(const fv_params &p, const DevParams &d, float *u1, float *u2, flo
     }
 }
 
+}  // namespace
+
+namespace fvgb {
+DevParams dev_params_of(const fv_params &p) { return make_dev_params(p); }
+int strip_cols() { return 4 * kWarpCols; }
+fv_status validate_params(const fv_params *p) { return validate(p); }
+void init_state_host(const fv_params &p, float *u1, float *u2, float *u3) {
+  init_host(p, make_dev_params(p), u1, u2, u3);
+}
+}  // namespace fvgb
+
+namespace {
+
 float *field_ptr(fv_handle *h, int buf, int f) {
   return h->state_mem + (size_t(buf) * 3 + size_t(f)) * h->field_stride;
 }
@@ -249,6 +272,16 @@ fv_status enqueue_attempts(fv_handle *h, long long n) {
     if (rc != 0) return fail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
   }
   return FV_OK;
+}
+
+// Four waves of resident CTAs, but no fewer than kMinRowsPerBlock strip-rows
+// per CTA (small grids). A warp of the step kernel is latency-bound, so an
+// SM runs at the speed of its resident warps: with one wave, SMs whose CTAs
+// finish early idle until the slowest CTA is done, while later waves keep
+// every SM full to the end (measured on 4096x2048: 4 waves 14% faster than
+// one, despite the extra halo rows of the shorter segments).
+long long default_blocks(int max_resident, long long work) {
+  return std::max(1LL, std::min(4LL * max_resident, work / kMinRowsPerBlock));
 }
 
 fv_status reset_ctrl(fv_handle *h) {
@@ -403,6 +436,9 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   };
   cudaError_t e = cudaMalloc(&h->state_mem, 6 * h->field_stride * sizeof(float));
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc state: %s", cudaGetErrorString(e)));
+  const size_t fcells = size_t(frame_cells(p->nx, p->ny));
+  e = cudaMalloc(&h->frame_mem, 3 * fcells * sizeof(float));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc frame: %s", cudaGetErrorString(e)));
   e = cudaMalloc(&h->ctrl, sizeof(Ctrl));
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc ctrl: %s", cudaGetErrorString(e)));
   e = cudaMallocHost(&h->ctrl_host, sizeof(Ctrl));
@@ -417,15 +453,17 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
   const long long work = (long long)nstrips * p->ny;
   const int per_sm = h->exact ? max_blocks_per_sm_exact(h->warps, -1) : max_blocks_per_sm_fast(h->warps, -1);
-  long long blocks = (long long)per_sm * prop.multiProcessorCount;
-  blocks = std::min(blocks, std::max(1LL, work / kMinRowsPerBlock));
-  e = cudaMalloc(&h->partials, size_t(blocks) * sizeof(float));
+  h->max_resident = per_sm * prop.multiProcessorCount;
+  long long blocks = default_blocks(h->max_resident, work);
+  h->partials_cap = std::max(h->max_resident, 1) * 8;
+  e = cudaMalloc(&h->partials, size_t(h->partials_cap) * sizeof(float));
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc partials: %s", cudaGetErrorString(e)));
 
   StepArgs &a = h->args;
   a.p = h->dp;
   for (int b = 0; b < 2; ++b)
     for (int f = 0; f < 3; ++f) a.state[b][f] = field_ptr(h, b, f);
+  for (int f = 0; f < 3; ++f) a.frame[f] = h->frame_mem + size_t(f) * fcells;
   a.ctrl = h->ctrl;
   a.partials = h->partials;
   a.nstrips = nstrips;
@@ -446,6 +484,7 @@ fv_status fv_destroy(fv_handle *h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->state_mem) cudaFree(h->state_mem);
   if (h->dbg_mem) cudaFree(h->dbg_mem);
+  if (h->frame_mem) cudaFree(h->frame_mem);
   if (h->ctrl) cudaFree(h->ctrl);
   if (h->ctrl_host) cudaFreeHost(h->ctrl_host);
   if (h->partials) cudaFree(h->partials);
@@ -567,6 +606,26 @@ fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out) {
   fill_stats(h, out);
   const int st = h->ctrl_host->status;
   if (st) return fail((fv_status)st, "device run stopped with status %d", st);
+  return FV_OK;
+}
+
+fv_status fv_set_launch(fv_handle *h, int32_t blocks) {
+  if (!h || blocks < 0) return fail(FV_BAD_ARG, "bad argument");
+  const long long b = blocks == 0 ? default_blocks(h->max_resident, h->args.work) : blocks;
+  if (b > h->partials_cap) return fail(FV_BAD_ARG, "blocks %lld above %d", b, h->partials_cap);
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  h->args.nblocks = int(b);
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return FV_OK;
+}
+
+fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (blocks) *blocks = h->args.nblocks;
+  if (max_resident) *max_resident = h->max_resident;
   return FV_OK;
 }
 

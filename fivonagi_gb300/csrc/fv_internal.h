@@ -22,6 +22,8 @@ struct DevParams {
   int32_t cfl_even_only;
   int32_t hifu_width;     // static_cast<int>(ISPa/dy), apps/hifu-beam/boundary.h:78
   int32_t max_retries;
+  int32_t moving_domain;
+  float mdvx, mdvy;       // MDVX, MDVY (mdt below)
   float dx, dy;
   float beta, diffdelta, cflmax, cflwhish;
   float ampl, frec, ispw;  // ISPW = Num2*PI*FREC
@@ -54,9 +56,23 @@ struct Ctrl {
   uint32_t pad;
 };
 
+// Ghost frame: the boundary hook's values of the ghost cells (the two
+// outermost rows and columns), written by a small pre-pass each attempt and
+// read by the step kernel in place of the state's own ghost cells. Layout:
+// rows j = 0, 1, ny-2, ny-1 (corners included) as four rows of nx, then the
+// left and right column pairs as [j][2] blocks of ny each.
+__host__ __device__ __forceinline__ int frame_cells(int nx, int ny) { return 4 * nx + 4 * ny; }
+__host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny) {
+  if (j <= 1) return j * nx + i;
+  if (j >= ny - 2) return (j - ny + 4) * nx + i;
+  if (i <= 1) return 4 * nx + 2 * j + i;
+  return 4 * nx + 2 * ny + 2 * j + (i - nx + 2);
+}
+
 struct StepArgs {
   DevParams p;
   float *state[2][3];     // two full state buffers (u1, u2, u3 each)
+  float *frame[3];        // ghost frame (see frame_index)
   Ctrl *ctrl;
   float *partials;        // one CFL maximum per CTA
   float *dbg[3];          // debug-stage output (stage kernels only)
@@ -65,10 +81,26 @@ struct StepArgs {
   int64_t work;           // nstrips * ny: strip-rows to share among the CTAs
 };
 
-// Launch configuration picked for a grid size.
-struct LaunchCfg {
-  int warps;              // warps per CTA
-  int blocks;             // CTAs per launch
+// One simulation of a batch: its parameters, buffers and control block,
+// and where its strip-rows start in the batch's concatenated work.
+struct BatchInst {
+  DevParams p;
+  float *state[2][3];
+  float *frame[3];
+  Ctrl *ctrl;
+  int64_t work_begin;     // first strip-row of this instance in the batch
+  int64_t work;           // nstrips * ny
+};
+
+struct BatchArgs {
+  const BatchInst *inst;  // device array of n instances
+  uint32_t *cfl_bits;     // per instance: running max CFL as float bits (non-negative)
+  int32_t *neg;           // per instance: a Riemann solve met tmp3 < 0
+  unsigned long long *done;  // per instance: strip-rows finished this attempt
+  int32_t n;
+  int32_t nblocks;
+  int64_t work;           // total strip-rows
+  int32_t max_frame;      // largest frame pre-pass work of an instance
 };
 
 // Launchers, one translation unit per arithmetic variant:
@@ -77,5 +109,16 @@ int launch_step_exact(const StepArgs &a, int warps, int stage, void *stream);
 int launch_step_fast(const StepArgs &a, int warps, int stage, void *stream);
 int max_blocks_per_sm_exact(int warps, int stage);
 int max_blocks_per_sm_fast(int warps, int stage);
+int launch_batch_exact(const BatchArgs &a, void *stream);
+int launch_batch_fast(const BatchArgs &a, void *stream);
+int max_batch_blocks_per_sm_exact();
+int max_batch_blocks_per_sm_fast();
+
+// Shared by the C-ABI translation units (fv_api.cu).
+DevParams dev_params_of(const fv_params &p);
+fv_status validate_params(const fv_params *p);
+void init_state_host(const fv_params &p, float *u1, float *u2, float *u3);
+void set_last_error(const char *msg);
+int strip_cols();  // output columns per strip of the step kernel
 
 }  // namespace fvgb

@@ -77,14 +77,14 @@ __device__ __forceinline__ void store3(float *const *out, int o, const Cell3 &v)
 // Warm-up and drain iterations compute on rows outside [y0-1, y1] and
 // discard the results (stores and flags are predicated), which keeps the
 // loop body free of branches.
-// EDGE: the warp's columns or rows include ghost cells, whose boundary-hook
-// values replace the loaded ones.
+// EDGE: the warp's columns include ghost columns.
 // STAGE < 0: full step into `out`; STAGE 0..3: that stage's grid into `out`.
 template <int STAGE, bool EDGE>
 __device__ __forceinline__ void stream_strip(const DevParams &p, const float *const *in,
+                                             const float *const *frame,
                                              float *const *out, int xw, int y0, int y1,
-                                             float dt, float T, int mdx, int mdy, float &cmax,
-                                             bool &neg) {
+                                             float dt, float T, int mdx, int mdy, int shx,
+                                             int shy, float &cmax, bool &neg) {
   const int lane = threadIdx.x & (kLanes - 1);
   const int nx = p.nx, ny = p.ny;
   const int i = xw - kHalo + lane;
@@ -96,9 +96,10 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   const float ddtx2 = p.diffdelta * dt / (p.dx * p.dx);
   const float ddty2 = p.diffdelta * dt / (p.dy * p.dy);
   const float two_bm1 = 2.0f * (p.beta - 1.0f);
-  const Ghost g{in[0], in[1], in[2], nx};
   const int ci = col_ok ? i : 0;
   const bool even_only = p.cfl_even_only != 0;
+  const float *const i0 = in[0], *const i1 = in[1], *const i2 = in[2];
+  const float *const f0 = frame[0], *const f1 = frame[1], *const f2 = frame[2];
 
   // ---- carried state (names give the row relative to the loaded row r)
   Cell3 s0_m2{0.f, 0.f, 0.f}, s0_m1{0.f, 0.f, 0.f};  // boundary-applied state
@@ -113,12 +114,16 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   Cell3 s2_m4{0.f, 0.f, 0.f}, s2_m5{0.f, 0.f, 0.f};  // S2 of rows r-4, r-5
   float vx2_m4 = 0.f, vy2_m4 = 0.f, vx2_m5 = 0.f, vy2_m5 = 0.f, vx2_m6 = 0.f, vy2_m6 = 0.f;
 
+  // Row r of the state after the boundary hook: ghost cells come from the
+  // ghost frame. Warps without ghost columns only meet ghost rows, which
+  // are the same for the whole warp.
   auto load_raw = [&](int r, Cell3 &v) {
     if (col_ok && r >= 0 && r < ny) {
-      const int o = ci + r * nx;
-      v.u1 = __ldg(in[0] + o);
-      v.u2 = __ldg(in[1] + o);
-      v.u3 = __ldg(in[2] + o);
+      const bool gh = EDGE ? is_ghost(p, i, r) : (r <= 1 || r >= ny - 2);
+      const int o = gh ? frame_index(ci, r, nx, ny) : ci + r * nx;
+      v.u1 = __ldg((gh ? f0 : i0) + o);
+      v.u2 = __ldg((gh ? f1 : i1) + o);
+      v.u3 = __ldg((gh ? f2 : i2) + o);
     } else {
       v = Cell3{0.f, 0.f, 0.f};
     }
@@ -132,14 +137,11 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     Cell3 u = pf0;
     pf0 = pf1;
     if (r + 2 <= y1 + 2) load_raw(r + 2, pf1);
-    if (EDGE) {
-      if (col_ok && r >= 0 && r < ny && is_ghost(p, i, r)) ghost_value(p, g, i, r, T, mdx, mdy, u.u1, u.u2, u.u3);
-    }
 
     // ======== Y chain: interface r, flux r-1, update of row r-2
     const float rho = u.u1 + 1.0f;
-    const float vx = u.u2 / rho;
-    const float vy = u.u3 / rho;
+    const float vx = fdiv(u.u2, rho);
+    const float vy = fdiv(u.u3, rho);
     WaveN w;
     Fluct f;
     float cy = 0.0f;
@@ -170,8 +172,8 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     // ======== X chain: row r-3; normal = u2, transverse = u3
     const int cxr = r - 3;
     const float rho1 = s1_m3.u1 + 1.0f;
-    const float vn1 = s1_m3.u2 / rho1;
-    const float vt1 = s1_m3.u3 / rho1;
+    const float vn1 = fdiv(s1_m3.u2, rho1);
+    const float vt1 = fdiv(s1_m3.u3, rho1);
     const float rho1m = shup(rho1), u2m = shup(s1_m3.u2), u3m = shup(s1_m3.u3);
     const float vn1m = shup(vn1), vt1m = shup(vt1);
     WaveN wx;
@@ -203,8 +205,8 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       s2.u3 = in_x ? m3 - dtx * (fxn3 - fx3) : s1_m3.u3;
     }
     const float rho2 = s2.u1 + 1.0f;
-    const float vx2 = s2.u2 / rho2;
-    const float vy2 = s2.u3 / rho2;
+    const float vx2 = fdiv(s2.u2, rho2);
+    const float vy2 = fdiv(s2.u3, rho2);
     {
       // CFL of cell (i, r-3): its y and x interfaces; 0 on i == 0
       const float cell = (i == 0) ? 0.0f : cx;
@@ -229,7 +231,18 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       o3.u3 = in_d ? s2_m5.u3 + ddtx2 * (vyl - 2.0f * vy2_m5 + vyr) +
                          ddty2 * (vy2_m6 - 2.0f * vy2_m5 + vy2_m4)
                    : s2_m5.u3;
-      if (out_lane && cdr >= y0 && cdr < y1) store3(out, i + cdr * nx, o3);
+      if (out_lane && cdr >= y0 && cdr < y1) {
+        if (STAGE < 0) {
+          // moving window (moveDomain, common/main.cu:109-164): the new
+          // cell (i - shx, j - shy) takes this cell's value, and a cell
+          // whose source would lie past the far edge keeps its own value
+          const int ti = i - shx, tj = cdr - shy;
+          if (ti >= 0 && tj >= 0) store3(out, ti + tj * nx, o3);
+          if (i + shx > nx - 1 || cdr + shy > ny - 1) store3(out, i + cdr * nx, o3);
+        } else {
+          store3(out, i + cdr * nx, o3);
+        }
+      }
     }
 
     // ======== rotate
@@ -254,8 +267,60 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   }
 }
 
-// Reduce the partial CFL maxima, accept or reject, update dt/T/n/cur.
-// Runs on the last CTA of the launch (all its threads).
+// Accept or reject an attempt from its CFL, and update dt/T/n/cur/MDX/MDY
+// (reduceCFL2, update_T, updateMDXY and update_dt of common/main.cu:166-230).
+// One thread; the control block is not read by anyone else until the next
+// launch.
+__device__ void decide(volatile Ctrl *vc, const DevParams &p, float cfl, bool negative) {
+  const float dt = vc->dt;
+  vc->last_cfl = cfl;
+  if (negative) {
+    vc->status = FV_NEGATIVE_EIGENVALUE;
+    vc->neg_flag = 0;
+    return;
+  }
+  int sim_error = 0;
+  if (cfl < p.cflmax) {  // reduceCFL2, common/main.cu:200-212
+    const float Tn = vc->T + dt;  // update_T, main.cu:232-238
+    vc->T = Tn;
+    vc->n = vc->n + 1;
+    if (p.moving_domain && Tn >= p.mdt) {  // updateMDXY, main.cu:166-177
+      const int mx = vc->mdx, my = vc->mdy;
+      vc->mdx = mx + (static_cast<int>((Tn - p.mdt) * p.mdvx / p.dx) - mx);
+      vc->mdy = my + (static_cast<int>((Tn - p.mdt) * p.mdvy / p.dy) - my);
+    }
+    vc->cur = vc->cur ^ 1;
+    vc->remaining = vc->remaining - 1;
+    vc->accepted = vc->accepted + 1;
+    vc->consecutive_rejects = 0;
+  } else {
+    sim_error = 1;
+    vc->rejected = vc->rejected + 1;
+    const int cr = vc->consecutive_rejects + 1;
+    vc->consecutive_rejects = cr;
+    if (cr >= p.max_retries) vc->status = FV_DT_TOO_LARGE;
+  }
+  vc->sim_error = sim_error;
+  // update_dt, main.cu:214-230 (the 0.9 is a double literal)
+  const float new_dt = dt * p.cflwhish / cfl;
+  if (sim_error == 1 && (double)new_dt > (double)dt * 0.9)
+    vc->dt = (float)((double)dt * 0.9);
+  else
+    vc->dt = new_dt;
+}
+
+// Whether an attempt runs: the run has steps left, no error, T < t_stop.
+// The control block only changes between launches, so every CTA of a
+// launch sees the same answer.
+__device__ __forceinline__ bool attempt_active(const Ctrl *ctl) {
+  const int status = __ldcg(&ctl->status);
+  const long long remaining = __ldcg((const long long *)&ctl->remaining);
+  const float T0 = __ldcg(&ctl->T), ts = __ldcg(&ctl->t_stop);
+  return status == 0 && remaining > 0 && T0 < ts;
+}
+
+// Reduce the partial CFL maxima and decide; runs on the last CTA of the
+// launch (all its threads).
 __device__ void finalize(const StepArgs &a, float *red) {
   Ctrl *ctl = a.ctrl;
   float m = 0.0f;
@@ -267,36 +332,7 @@ __device__ void finalize(const StepArgs &a, float *red) {
   float cfl = 0.0f;
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) cfl = nanmax(cfl, red[w]);
   volatile Ctrl *vc = ctl;
-  const float dt = vc->dt;
-  vc->last_cfl = cfl;
-  if (vc->neg_flag) {
-    vc->status = FV_NEGATIVE_EIGENVALUE;
-    vc->neg_flag = 0;
-    vc->blocks_done = 0;
-    return;
-  }
-  int sim_error = 0;
-  if (cfl < a.p.cflmax) {  // reduceCFL2, common/main.cu:200-212
-    vc->T = vc->T + dt;    // update_T, main.cu:232-238
-    vc->n = vc->n + 1;
-    vc->cur = vc->cur ^ 1;
-    vc->remaining = vc->remaining - 1;
-    vc->accepted = vc->accepted + 1;
-    vc->consecutive_rejects = 0;
-  } else {
-    sim_error = 1;
-    vc->rejected = vc->rejected + 1;
-    const int cr = vc->consecutive_rejects + 1;
-    vc->consecutive_rejects = cr;
-    if (cr >= a.p.max_retries) vc->status = FV_DT_TOO_LARGE;
-  }
-  vc->sim_error = sim_error;
-  // update_dt, main.cu:214-230 (the 0.9 is a double literal)
-  const float new_dt = dt * a.p.cflwhish / cfl;
-  if (sim_error == 1 && (double)new_dt > (double)dt * 0.9)
-    vc->dt = (float)((double)dt * 0.9);
-  else
-    vc->dt = new_dt;
+  decide(vc, a.p, cfl, vc->neg_flag != 0);
   __threadfence();
   vc->blocks_done = 0;
 }
@@ -308,18 +344,23 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   __shared__ int is_last;
   const Ctrl *ctl = a.ctrl;
   // Uniform early exit: the control block only changes between launches.
-  if (STAGE < 0) {
-    const int status = __ldcg(&ctl->status);
-    const long long remaining = __ldcg((const long long *)&ctl->remaining);
-    const float T0 = __ldcg(&ctl->T), ts = __ldcg(&ctl->t_stop);
-    if (status != 0 || remaining <= 0 || !(T0 < ts)) return;
-  }
+  if (STAGE < 0 && !attempt_active(ctl)) return;
   if (threadIdx.x == 0) neg_any = 0;
   __syncthreads();
   const float dt = __ldcg(&ctl->dt);
   const float T = __ldcg(&ctl->T);
   const int cur = __ldcg(&ctl->cur);
   const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
+  // Window shift this attempt applies if it is accepted: updateMDXY with the
+  // updated T (common/main.cu:126-137, 166-177); 0 before MDT.
+  int shx = 0, shy = 0;
+  if (STAGE < 0 && a.p.moving_domain) {
+    const float Tn = T + dt;
+    if (Tn >= a.p.mdt) {
+      shx = static_cast<int>((Tn - a.p.mdt) * a.p.mdvx / a.p.dx) - mdx;
+      shy = static_cast<int>((Tn - a.p.mdt) * a.p.mdvy / a.p.dy) - mdy;
+    }
+  }
   const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
   float *out[3];
   for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
@@ -338,13 +379,13 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     const int y1 = (int)((long long)y0 + left < ny ? (long long)y0 + left : ny);
     const int xw = strip * kStripCols + warp * kWarpCols;
     if (xw < a.p.nx) {
-      // ghost cells among the loaded rows [y0-3, y1+2] or the warp's columns?
-      const bool edge = (y0 - 3 <= 1) || (y1 + 2 >= ny - 2) || (xw - kHalo <= 1) ||
-                        (xw + kLanes - kHalo - 1 >= a.p.nx - 2);
+      // ghost columns among the warp's 32 columns?
+      const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= a.p.nx - 2);
+      const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
       if (edge)
-        stream_strip<STAGE, true>(a.p, in, out, xw, y0, y1, dt, T, mdx, mdy, cmax, neg);
+        stream_strip<STAGE, true>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
       else
-        stream_strip<STAGE, false>(a.p, in, out, xw, y0, y1, dt, T, mdx, mdy, cmax, neg);
+        stream_strip<STAGE, false>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
     }
     pos += y1 - y0;
   }
@@ -371,10 +412,174 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   }
 }
 
+// The app's boundary hook (boundary(), apps/*/boundary.h) evaluated for
+// frame cell k of one simulation: the four ghost rows first, then the left
+// and right ghost column pairs.
+__device__ __forceinline__ void frame_job(const DevParams &p, const float *const *state,
+                                          float *const *frame, int k, float T, int mdx, int mdy) {
+  const int nx = p.nx, ny = p.ny;
+  const int rows = 4 * nx, cols = 2 * (ny - 4);
+  int i, j;
+  if (k < rows) {
+    const int rr = k / nx;
+    i = k - rr * nx;
+    j = rr < 2 ? rr : ny - 4 + rr;
+  } else if (k < rows + cols) {
+    const int q = k - rows;
+    j = 2 + (q >> 1);
+    i = q & 1;
+  } else {
+    const int q = k - rows - cols;
+    j = 2 + (q >> 1);
+    i = nx - 2 + (q & 1);
+  }
+  const Ghost g{state[0], state[1], state[2], nx};
+  float v1, v2, v3;
+  ghost_value(p, g, i, j, T, mdx, mdy, v1, v2, v3);
+  const int o = frame_index(i, j, nx, ny);
+  frame[0][o] = v1;
+  frame[1][o] = v2;
+  frame[2][o] = v3;
+}
+
+__device__ __forceinline__ int frame_jobs(const DevParams &p) { return 4 * p.nx + 4 * (p.ny - 4); }
+
+// Pre-pass of each attempt: the ghost frame of the current state. Skips
+// like the step kernel does when the run is idle or stopped.
+__global__ void __launch_bounds__(256) ghost_frame_kernel(StepArgs a, int check_ctrl) {
+  const Ctrl *ctl = a.ctrl;
+  if (check_ctrl && !attempt_active(ctl)) return;
+  const float T = __ldcg(&ctl->T);
+  const int cur = __ldcg(&ctl->cur);
+  const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
+  const int total = frame_jobs(a.p);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x)
+    frame_job(a.p, a.state[cur], a.frame, k, T, mdx, mdy);
+}
+
+// ---------------------------------------------------------------- batches
+
+// Ghost frames of every active simulation of a batch; blockIdx.y picks it.
+__global__ void __launch_bounds__(256) batch_frame_kernel(BatchArgs b) {
+  const BatchInst &I = b.inst[blockIdx.y];
+  if (!attempt_active(I.ctrl)) return;
+  const float T = __ldcg(&I.ctrl->T);
+  const int cur = __ldcg(&I.ctrl->cur);
+  const int mdx = __ldcg(&I.ctrl->mdx), mdy = __ldcg(&I.ctrl->mdy);
+  const DevParams p = I.p;
+  const int total = frame_jobs(p);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x)
+    frame_job(p, I.state[cur], I.frame, k, T, mdx, mdy);
+}
+
+// One attempted step of every active simulation of a batch (uneven grid
+// sizes and parameters) in one launch. CTAs share the batch's concatenated
+// (simulation, strip, row) space evenly. A CTA contributes its rows of one
+// simulation with an atomic max of their CFL (float bits of non-negative
+// values order like unsigned integers, and NaN above all) and an atomic
+// count of finished strip-rows; whoever completes a simulation's count
+// decides that simulation's attempt. No CTA waits on another.
+__global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
+  __shared__ float red[kWarps];
+  __shared__ int neg_any;
+  const int warp = threadIdx.x >> 5;
+  const long long W = b.work;
+  const long long bid = blockIdx.x;
+  const long long s0 = bid * W / b.nblocks, s1 = (bid + 1) * W / b.nblocks;
+  int k = 0;
+  while (k < b.n - 1 && b.inst[k + 1].work_begin <= s0) ++k;
+  long long pos = s0;
+  while (pos < s1 && k < b.n) {
+    const BatchInst &I = b.inst[k];
+    const long long kb = I.work_begin, ke = kb + I.work;
+    const long long seg_end = s1 < ke ? s1 : ke;
+    if (pos < seg_end && attempt_active(I.ctrl)) {
+      const DevParams p = I.p;
+      const Ctrl *ctl = I.ctrl;
+      const float dt = __ldcg(&ctl->dt);
+      const float T = __ldcg(&ctl->T);
+      const int cur = __ldcg(&ctl->cur);
+      const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
+      int shx = 0, shy = 0;
+      if (p.moving_domain) {
+        const float Tn = T + dt;
+        if (Tn >= p.mdt) {
+          shx = static_cast<int>((Tn - p.mdt) * p.mdvx / p.dx) - mdx;
+          shy = static_cast<int>((Tn - p.mdt) * p.mdvy / p.dy) - mdy;
+        }
+      }
+      const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
+      float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
+      const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
+      if (threadIdx.x == 0) neg_any = 0;
+      __syncthreads();
+      float cmax = 0.0f;
+      bool neg = false;
+      for (long long q = pos; q < seg_end;) {
+        const long long rel = q - kb;
+        const int strip = (int)(rel / p.ny);
+        const int y0 = (int)(rel - (long long)strip * p.ny);
+        const long long left = seg_end - q;
+        const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
+        const int xw = strip * kStripCols + warp * kWarpCols;
+        if (xw < p.nx) {
+          const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= p.nx - 2);
+          if (edge)
+            stream_strip<-1, true>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
+          else
+            stream_strip<-1, false>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
+        }
+        q += y1 - y0;
+      }
+      for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+      if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) neg_any = 1;
+      if ((threadIdx.x & 31) == 0) red[warp] = cmax;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float m = red[0];
+        for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
+        atomicMax(b.cfl_bits + k, __float_as_uint(m));
+        if (neg_any) atomicExch(b.neg + k, 1);
+        __threadfence();
+        const unsigned long long rows = (unsigned long long)(seg_end - pos);
+        const unsigned long long prev = atomicAdd(b.done + k, rows);
+        if (prev + rows == (unsigned long long)I.work) {
+          __threadfence();
+          const float cfl = __uint_as_float(atomicExch(b.cfl_bits + k, 0u));
+          const int negative = atomicExch(b.neg + k, 0);
+          b.done[k] = 0ull;
+          decide((volatile Ctrl *)I.ctrl, p, cfl, negative != 0);
+          __threadfence();
+        }
+      }
+      __syncthreads();
+    }
+    pos = seg_end;
+    ++k;
+  }
+}
+
+static int launch_batch_impl(const BatchArgs &b, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 fgrid((b.max_frame + 255) / 256, b.n);
+  batch_frame_kernel<<<fgrid, 256, 0, st>>>(b);
+  batch_step_kernel<<<b.nblocks, kThreads, 0, st>>>(b);
+  return (int)cudaGetLastError();
+}
+
+static int batch_occupancy() {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (void *)batch_step_kernel, kThreads, 0) != cudaSuccess)
+    return 1;
+  return nb > 0 ? nb : 1;
+}
+
 template <int STAGE> static void *kernel_ptr() { return (void *)step_kernel<STAGE>; }
 
 static int launch_impl(const StepArgs &a, int stage, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
+  const int ftotal = 4 * a.p.nx + 4 * (a.p.ny - 4);
+  ghost_frame_kernel<<<(ftotal + 255) / 256, 256, 0, st>>>(a, stage < 0 ? 1 : 0);
   dim3 grid(a.nblocks), block(kThreads);
   switch (stage) {
     case -1: step_kernel<-1><<<grid, block, 0, st>>>(a); break;
@@ -397,6 +602,8 @@ static int occupancy(int stage) {
 }  // namespace exact_ns / fast_ns
 
 #if FV_VARIANT_EXACT
+int launch_batch_exact(const BatchArgs &a, void *stream) { return exact_ns::launch_batch_impl(a, stream); }
+int max_batch_blocks_per_sm_exact() { return exact_ns::batch_occupancy(); }
 int launch_step_exact(const StepArgs &a, int warps, int stage, void *stream) {
   return warps == exact_ns::kWarps ? exact_ns::launch_impl(a, stage, stream)
                                    : (int)cudaErrorInvalidValue;
@@ -405,6 +612,8 @@ int max_blocks_per_sm_exact(int warps, int stage) {
   return warps == exact_ns::kWarps ? exact_ns::occupancy(stage) : 0;
 }
 #else
+int launch_batch_fast(const BatchArgs &a, void *stream) { return fast_ns::launch_batch_impl(a, stream); }
+int max_batch_blocks_per_sm_fast() { return fast_ns::batch_occupancy(); }
 int launch_step_fast(const StepArgs &a, int warps, int stage, void *stream) {
   return warps == fast_ns::kWarps ? fast_ns::launch_impl(a, stage, stream)
                                   : (int)cudaErrorInvalidValue;

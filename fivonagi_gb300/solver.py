@@ -115,8 +115,93 @@ class Simulation:
         check(self.lib.fv_sync(self.h, C.byref(st)), "fv_sync")
         return st.as_dict()
 
+    def set_launch(self, blocks: int) -> None:
+        """CTAs per step launch (0 = default); see fv_set_launch."""
+        check(self.lib.fv_set_launch(self.h, int(blocks)), "fv_set_launch")
+
+    def get_launch(self) -> tuple[int, int]:
+        """(CTAs per launch, CTAs resident at once on this device)."""
+        b, m = C.c_int32(), C.c_int32()
+        check(self.lib.fv_get_launch(self.h, C.byref(b), C.byref(m)), "fv_get_launch")
+        return b.value, m.value
+
     def debug_step(self, stage: int):
         """One step of the current state stopped after `stage` (no commit)."""
         out = [np.empty(self.shape, np.float32) for _ in range(3)]
         check(self.lib.fv_debug_step(self.h, int(stage), *[a.ctypes.data for a in out]), "fv_debug_step")
         return out
+
+
+class Batch:
+    """n independent simulations stepped together (fv_batch_*)."""
+
+    def __init__(self, params_list):
+        self.lib = _abi.load_library()
+        self.params = [p.copy() for p in params_list]
+        self.n = len(self.params)
+        arr = (FvParams * self.n)(*self.params)
+        h = C.c_void_p()
+        check(self.lib.fv_batch_create(self.n, arr, C.byref(h)), "fv_batch_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.fv_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shape(self, k: int):
+        return (self.params[k].ny, self.params[k].nx)
+
+    def init_state(self) -> None:
+        check(self.lib.fv_batch_init_state(self.h), "fv_batch_init_state")
+
+    def set_state(self, k: int, u1, u2, u3) -> None:
+        arrs = [np.ascontiguousarray(u, dtype=np.float32).reshape(self.shape(k)) for u in (u1, u2, u3)]
+        check(self.lib.fv_batch_set_state(self.h, k, *[a.ctypes.data for a in arrs], 0), "fv_batch_set_state")
+
+    def get_state(self, k: int):
+        out = [np.empty(self.shape(k), np.float32) for _ in range(3)]
+        check(self.lib.fv_batch_get_state(self.h, k, *[a.ctypes.data for a in out], 0), "fv_batch_get_state")
+        return out
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self.lib.fv_batch_set_stream(self.h, stream_ptr), "fv_batch_set_stream")
+
+    def run(self, nsteps: int) -> list[dict]:
+        st = (FvRunStats * self.n)()
+        check(self.lib.fv_batch_run(self.h, int(nsteps), st), "fv_batch_run")
+        return [s.as_dict() for s in st]
+
+    def run_status(self, nsteps: int) -> tuple[int, list[dict]]:
+        """Like run, but returns (status, stats) instead of raising."""
+        st = (FvRunStats * self.n)()
+        rc = self.lib.fv_batch_run(self.h, int(nsteps), st)
+        return rc, [s.as_dict() for s in st]
+
+    def launch_attempts(self, n: int) -> None:
+        check(self.lib.fv_batch_launch_attempts(self.h, int(n)), "fv_batch_launch_attempts")
+
+    def sync(self) -> list[dict]:
+        st = (FvRunStats * self.n)()
+        check(self.lib.fv_batch_sync(self.h, st), "fv_batch_sync")
+        return [s.as_dict() for s in st]
+
+    def set_launch(self, blocks: int) -> None:
+        check(self.lib.fv_batch_set_launch(self.h, int(blocks)), "fv_batch_set_launch")
+
+    def get_launch(self) -> tuple[int, int]:
+        b, m = C.c_int32(), C.c_int32()
+        check(self.lib.fv_batch_get_launch(self.h, C.byref(b), C.byref(m)), "fv_batch_get_launch")
+        return b.value, m.value

@@ -168,11 +168,50 @@ fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out);
 fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts);
 fv_status fv_sync(fv_handle *h, fv_run_stats *out);
 
+/* Launch shape of the step kernel, for the autotuner: `blocks` persistent
+ * CTAs share the grid's (strip, row) work evenly; 0 restores the default
+ * (four waves of resident CTAs, at most 8 waves). fv_get_launch reports the current value and
+ * how many CTAs fit on the device at once. No reference counterpart: the
+ * reference launches one thread per cell (common/main.cu:252-253). */
+fv_status fv_set_launch(fv_handle *h, int32_t blocks);
+fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident);
+
 /* One step of the current state, stopped after `stage`; writes the stage's
  * full grid to u1/u2/u3 (host pointers) and leaves the handle's state,
  * dt, T and n unchanged. For per-phase parity tests. */
 fv_status fv_debug_step(fv_handle *h, int32_t stage, float *u1, float *u2,
                         float *u3);
+
+/* ------------------------------------------------------------- batches
+ * n independent simulations, each with its own fv_params (app, grid size,
+ * physics), dt, T and CFL, stepped together: every launch attempts one step
+ * of each simulation that still has steps to take. No reference
+ * counterpart: the reference runs one simulation per process and its sweep
+ * scripts rebuild and rerun it per parameter point (apps/hifu-beam/run.sh:26-74). */
+typedef struct fv_batch fv_batch;
+
+/* All simulations of a batch share `exact`. */
+fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out);
+fv_status fv_batch_destroy(fv_batch *b);
+fv_status fv_batch_set_stream(fv_batch *b, void *cuda_stream);
+/* Every simulation's init hook; dt = DTINI, T = -TIDE, n = 0 for all. */
+fv_status fv_batch_init_state(fv_batch *b);
+/* State of simulation k (its own NX*NY floats per field); set_state also
+ * resets that simulation's dt, T, n. */
+fv_status fv_batch_set_state(fv_batch *b, int32_t k, const float *u1, const float *u2,
+                             const float *u3, int32_t on_device);
+fv_status fv_batch_get_state(fv_batch *b, int32_t k, float *u1, float *u2, float *u3,
+                             int32_t on_device);
+/* Every simulation takes exactly nsteps accepted steps; out[k] (n entries,
+ * optional) receives each one's stats. */
+fv_status fv_batch_run(fv_batch *b, int64_t nsteps, fv_run_stats *out);
+/* Enqueue nattempts attempts of every simulation without synchronising;
+ * fv_batch_sync waits and reports. */
+fv_status fv_batch_launch_attempts(fv_batch *b, int64_t nattempts);
+fv_status fv_batch_sync(fv_batch *b, fv_run_stats *out);
+/* CTAs of the batch launch (0 = default), for the autotuner. */
+fv_status fv_batch_set_launch(fv_batch *b, int32_t blocks);
+fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_resident);
 
 #ifdef __cplusplus
 }

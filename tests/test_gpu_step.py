@@ -139,12 +139,33 @@ def test_rejected_step_is_retried_like_the_oracle():
 
 
 def test_dt_too_large_after_retry_budget():
-    p = small_params(2, 64, 32).replace(dtini=5.0, max_retries=2)
+    # CFL ~1.3 on the first attempt: rejected, and with a retry budget of
+    # one attempt the run stops with simError 1 (dt too large)
+    p = small_params(2, 64, 32).replace(dtini=0.08, max_retries=1)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    assert orc.run(5)["rc"] == _abi.FV_DT_TOO_LARGE
     sim = Simulation(p)
     sim.init_state()
     with pytest.raises(_abi.FvError) as e:
         sim.run(5)
     assert e.value.status == _abi.FV_DT_TOO_LARGE
+    assert sim.stats()["rejected"] == 1
+    sim.close()
+
+
+def test_overshooting_dt_reports_negative_eigenvalue():
+    # dt 80x the cell crossing time: the y sweep drives rho negative and the
+    # x sweep's Riemann solve meets tmp3 < 0, as in the reference
+    p = small_params(2, 64, 32).replace(dtini=5.0, max_retries=2)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    assert orc.run(5)["rc"] == _abi.FV_NEGATIVE_EIGENVALUE
+    sim = Simulation(p)
+    sim.init_state()
+    with pytest.raises(_abi.FvError) as e:
+        sim.run(5)
+    assert e.value.status == _abi.FV_NEGATIVE_EIGENVALUE
     sim.close()
 
 
@@ -181,4 +202,23 @@ def test_run_until_matches_calc_frame_loop():
     g, o = sim.get_state(), orc.get_state()
     for f in range(3):
         assert same_values(g[f], o[f])
+    sim.close()
+
+
+@pytest.mark.parametrize("app,mdt,nsteps", [(1, 6.25, 90), (0, -1.0, 60), (2, 0.5, 60)])
+def test_moving_domain_matches_oracle(app, mdt, nsteps):
+    """The window shift of moveDomain/updateMDXY once T >= MDT."""
+    p = small_params(app, 64, 32).replace(moving_domain=1, mdt=mdt, mdvx=1.0, mdvy=0.25)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    u = perturbed(orc.get_state(), 3, 1e-4)
+    orc.set_state(*u)
+    so = orc.run(nsteps)
+    sim = Simulation(p)
+    sim.set_state(*u)
+    sg = sim.run(nsteps)
+    assert so["mdx"] > 0 and sg["mdx"] == so["mdx"] and sg["mdy"] == so["mdy"]
+    g, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
     sim.close()
