@@ -122,6 +122,18 @@ class FvRunStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class FvStepResult(C.Structure):
+    _fields_ = [
+        ("accepted", C.c_int32),
+        ("status", C.c_int32),
+        ("cfl", C.c_double),
+        ("dt_next", C.c_double),
+        ("T", C.c_double),
+        ("mdx", C.c_int32),
+        ("mdy", C.c_int32),
+    ]
+
+
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
 
@@ -156,6 +168,8 @@ PROTOTYPES = {
     "fv_batch_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_batch_set_launch": (C.c_int, [_P, C.c_int32]),
     "fv_batch_get_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "fv_step_noalloc": (C.c_int, [C.POINTER(FvParams), _P, _P, _P, _P, _P, _P, C.c_double, C.c_double,
+                                  C.c_int32, C.c_int32, _P, C.POINTER(FvStepResult)]),
 }
 
 _lib = None

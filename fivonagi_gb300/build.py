@@ -5,6 +5,7 @@ Translation units, compiled in parallel:
   fv_step.cu (fast)   --fmad=true : contracted FMAs, checked against the FP32 tolerance
   fv_api.cu           the C ABI of one simulation (host code, control-block kernels)
   fv_batch.cu         the C ABI of batches
+  fv_noalloc.cu       one step attempt with no device allocation
 """
 from __future__ import annotations
 
@@ -39,6 +40,7 @@ def _units():
         ("fv_step_fast.o", step, ["-DFV_VARIANT_EXACT=0", "--fmad=true"]),
         ("fv_api.o", os.path.join(CSRC, "fv_api.cu"), []),
         ("fv_batch.o", os.path.join(CSRC, "fv_batch.cu"), []),
+        ("fv_noalloc.o", os.path.join(CSRC, "fv_noalloc.cu"), []),
     ]
 
 

@@ -1,0 +1,165 @@
+// fv_noalloc.cu -- one step attempt without any device allocation.
+//
+// Some callers of this library cannot let it call cudaMalloc: programs that
+// hand all device memory to one allocator of their own (a framework's
+// caching allocator, or a fixed arena sized at start-up) would see a
+// library allocation bypass their accounting, or fail outright once the
+// arena holds the whole device. fv_step_noalloc serves them: the caller
+// passes the input and output state buffers, and the step kernel's scratch
+// (control block, per-CTA CFL maxima, ghost frame) lives in one file-scope
+// __device__ array of fixed size instead of fv_create's allocations.
+//
+// The array is FV_NOALLOC_SCRATCH_BYTES per device; every GPU that loads the
+// library holds it until the process exits. All calls on a device share it,
+// so calls that overlap on the GPU (two streams, or a call issued before
+// the previous one finished) race on it and must be serialised by the
+// caller. The first call on each device looks up the array's device address
+// (cudaGetSymbolAddress), so make that first call before any stream capture.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <mutex>
+
+#include "fv_internal.h"
+
+using namespace fvgb;
+
+namespace {
+
+constexpr int kNoallocMaxCtas = FV_NOALLOC_MAX_CTAS;
+constexpr int kNoallocMaxFrame = 4 * FV_NOALLOC_MAX_PERIMETER;  // frame_cells(nx, ny) <= this
+constexpr size_t kCtrlBytes = 256;                               // Ctrl, padded
+constexpr size_t kPartialBytes = size_t(kNoallocMaxCtas) * sizeof(float);
+constexpr size_t kFrameBytes = 3 * size_t(kNoallocMaxFrame) * sizeof(float);
+static_assert(sizeof(Ctrl) <= kCtrlBytes, "control block does not fit its slot");
+static_assert(kCtrlBytes + kPartialBytes + kFrameBytes <= FV_NOALLOC_SCRATCH_BYTES,
+              "scratch layout exceeds FV_NOALLOC_SCRATCH_BYTES");
+
+// The scratch itself: a host-side stand-in in host code, a real array on
+// every device. Host code must use the address from cudaGetSymbolAddress.
+__device__ __align__(256) unsigned char g_noalloc_scratch[FV_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char *g_scratch_addr[kMaxDevices] = {};
+int g_max_resident[kMaxDevices] = {};
+
+// Errors go to the library's per-thread message (fv_last_error_string).
+fv_status nafail(fv_status s, const char *msg, cudaError_t e = cudaSuccess) {
+  char buf[256];
+  if (e != cudaSuccess)
+    snprintf(buf, sizeof(buf), "fv_step_noalloc: %s: %s", msg, cudaGetErrorString(e));
+  else
+    snprintf(buf, sizeof(buf), "fv_step_noalloc: %s", msg);
+  set_last_error(buf);
+  return s;
+}
+
+// Writes every control-block field the step kernel reads or counts with,
+// so the previous call's contents never leak into this one.
+__global__ void noalloc_begin_kernel(Ctrl *c, float dt, float T, int mdx, int mdy, int max_retries) {
+  c->dt = dt;
+  c->T = T;
+  c->last_cfl = 0.0f;
+  c->t_stop = __int_as_float(0x7f800000);
+  c->n = 0;
+  c->cur = 0;
+  c->status = 0;
+  c->neg_flag = 0;
+  c->sim_error = 0;
+  c->consecutive_rejects = 0;
+  c->mdx = mdx;
+  c->mdy = mdy;
+  c->remaining = 1;
+  c->accepted = 0;
+  c->rejected = 0;
+  c->blocks_done = 0u;
+  (void)max_retries;
+}
+
+}  // namespace
+
+extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, const float *in_u2,
+                                     const float *in_u3, float *out_u1, float *out_u2,
+                                     float *out_u3, double dt, double T, int32_t mdx,
+                                     int32_t mdy, void *cuda_stream, fv_step_result *res) {
+  if (!p || !in_u1 || !in_u2 || !in_u3 || !out_u1 || !out_u2 || !out_u3 || !res)
+    return nafail(FV_BAD_ARG, "NULL argument");
+  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM) return nafail(FV_BAD_ARG, "unknown app");
+  if (p->nx < 8 || p->ny < 8) return nafail(FV_BAD_ARG, "grid below 8x8");
+  if ((long long)p->nx + (long long)p->ny > FV_NOALLOC_MAX_PERIMETER)
+    return nafail(FV_BAD_ARG, "nx + ny above FV_NOALLOC_MAX_PERIMETER (the ghost frame's room in the scratch array)");
+  if ((long long)p->nx * (long long)p->ny > (1LL << 30)) return nafail(FV_BAD_ARG, "grid above 2^30 cells");
+  if (!(p->xmax > 0) || !(p->ymax > 0) || !(dt > 0)) return nafail(FV_BAD_ARG, "xmax, ymax and dt must be positive");
+  if (p->moving_domain && (p->mdvx < 0 || p->mdvy < 0)) return nafail(FV_BAD_ARG, "mdvx, mdvy must be >= 0");
+
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return nafail(FV_NO_DEVICE, "cudaGetDevice", e);
+  if (dev < 0 || dev >= kMaxDevices) return nafail(FV_NO_DEVICE, "device index out of range");
+  unsigned char *base = nullptr;
+  int max_resident = 0;
+  {
+    // Set-up, once per device, with that device current.
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev]) {
+      cudaDeviceProp prop;
+      e = cudaGetDeviceProperties(&prop, dev);
+      if (e != cudaSuccess) return nafail(FV_NO_DEVICE, "cudaGetDeviceProperties", e);
+      if (prop.major != 10 || prop.minor != 3) return nafail(FV_NO_DEVICE, "not an sm_103 device");
+      void *ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) return nafail(FV_CUDA_ERROR, "cudaGetSymbolAddress(scratch)", e);
+      const int per_sm = p->exact ? max_blocks_per_sm_exact(4, -1) : max_blocks_per_sm_fast(4, -1);
+      g_max_resident[dev] = per_sm * prop.multiProcessorCount;
+      g_scratch_addr[dev] = static_cast<unsigned char *>(ptr);
+    }
+    base = g_scratch_addr[dev];
+    max_resident = g_max_resident[dev];
+  }
+
+  StepArgs a{};
+  a.p = dev_params_of(*p);
+  const int strip_cols = 4 * kWarpCols;
+  const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
+  const long long work = (long long)nstrips * p->ny;
+  long long blocks = std::max(1LL, std::min(4LL * max_resident, work / 32));
+  if (blocks > kNoallocMaxCtas) blocks = kNoallocMaxCtas;
+  Ctrl *ctrl = reinterpret_cast<Ctrl *>(base);
+  float *partials = reinterpret_cast<float *>(base + kCtrlBytes);
+  float *frame = reinterpret_cast<float *>(base + kCtrlBytes + kPartialBytes);
+  const size_t fcells = size_t(frame_cells(p->nx, p->ny));
+  a.state[0][0] = const_cast<float *>(in_u1);
+  a.state[0][1] = const_cast<float *>(in_u2);
+  a.state[0][2] = const_cast<float *>(in_u3);
+  a.state[1][0] = out_u1;
+  a.state[1][1] = out_u2;
+  a.state[1][2] = out_u3;
+  for (int f = 0; f < 3; ++f) a.frame[f] = frame + size_t(f) * fcells;
+  a.ctrl = ctrl;
+  a.partials = partials;
+  a.nstrips = nstrips;
+  a.nblocks = int(blocks);
+  a.work = work;
+
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  noalloc_begin_kernel<<<1, 1, 0, st>>>(ctrl, float(dt), float(T), mdx, mdy, a.p.max_retries);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return nafail(FV_CUDA_ERROR, "control-block launch", e);
+  const int rc = p->exact ? launch_step_exact(a, 4, -1, st) : launch_step_fast(a, 4, -1, st);
+  if (rc != 0) return nafail(FV_CUDA_ERROR, "step launch", (cudaError_t)rc);
+  Ctrl c;
+  e = cudaMemcpyAsync(&c, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return nafail(FV_CUDA_ERROR, "reading the control block", e);
+  res->accepted = c.accepted > 0 ? 1 : 0;
+  res->status = c.status;
+  res->cfl = c.last_cfl;
+  res->dt_next = c.dt;
+  res->T = c.T;
+  res->mdx = c.mdx;
+  res->mdy = c.mdy;
+  if (c.status == FV_NEGATIVE_EIGENVALUE) return nafail(FV_NEGATIVE_EIGENVALUE, "negative eigenvalue (tmp3 < 0)");
+  return FV_OK;
+}

@@ -213,6 +213,41 @@ fv_status fv_batch_sync(fv_batch *b, fv_run_stats *out);
 fv_status fv_batch_set_launch(fv_batch *b, int32_t blocks);
 fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_resident);
 
+/* ------------------------------------------------- step without allocation
+ * For callers that cannot let this library call cudaMalloc: programs whose
+ * device memory belongs to one allocator of their own (a framework's
+ * caching allocator, or an arena sized at start-up) would have a library
+ * allocation bypass their accounting, or fail once the arena holds the
+ * device. fv_step_noalloc attempts one step of `p`'s simulation from the
+ * caller's input state into the caller's output state (NX*NY device floats
+ * per field each) at time T with step dt and window offsets mdx, mdy, and
+ * allocates nothing: the step kernel's scratch (control block, per-CTA CFL
+ * maxima, ghost frame) is one fixed __device__ array of
+ * FV_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits. Limit: nx + ny <= FV_NOALLOC_MAX_PERIMETER; larger grids
+ * are rejected with FV_BAD_ARG. All calls on a device share the array, so
+ * calls that overlap on the GPU race: serialise them. The first call on
+ * each device looks up the array's address, so make it before any stream
+ * capture. res->accepted = 0 means CFL >= CFLMAX: retry from the same input
+ * with res->dt_next. No reference counterpart. */
+#define FV_NOALLOC_SCRATCH_BYTES (800u * 1024u)
+#define FV_NOALLOC_MAX_CTAS 2048
+#define FV_NOALLOC_MAX_PERIMETER 16384
+
+typedef struct fv_step_result {
+  int32_t accepted;       /* 1: output holds the new state; 0: rejected (retry) */
+  int32_t status;         /* fv_status of the attempt */
+  double cfl;             /* CFL of the attempt */
+  double dt_next;         /* dt for the next attempt (update_dt) */
+  double T;               /* time after the attempt */
+  int32_t mdx, mdy;       /* window offsets after the attempt */
+} fv_step_result;
+
+fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, const float *in_u2,
+                          const float *in_u3, float *out_u1, float *out_u2, float *out_u3,
+                          double dt, double T, int32_t mdx, int32_t mdy, void *cuda_stream,
+                          fv_step_result *res);
+
 #ifdef __cplusplus
 }
 #endif
