@@ -99,6 +99,7 @@ struct fv_handle {
   Ctrl *ctrl = nullptr;
   Ctrl *ctrl_host = nullptr;    // pinned mirror for reads
   float *partials = nullptr;
+  uint32_t *fix = nullptr;      // fix-up scratch of the step launches
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -456,8 +457,13 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   h->max_resident = per_sm * prop.multiProcessorCount;
   long long blocks = default_blocks(h->max_resident, work);
   h->partials_cap = std::max(h->max_resident, 1) * 8;
-  e = cudaMalloc(&h->partials, size_t(h->partials_cap) * sizeof(float));
+  // the fix-up launch: four CTAs per SM (its occupancy) take the marked chunks
+  const int fix_blocks = 4 * prop.multiProcessorCount;
+  e = cudaMalloc(&h->partials, size_t(h->partials_cap + fix_blocks) * sizeof(float));
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc partials: %s", cudaGetErrorString(e)));
+  const size_t fix_words = size_t(fix_scratch_words((long long)nstrips * h->warps, p->ny));
+  e = cudaMalloc(&h->fix, fix_words * sizeof(uint32_t));
+  if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc fix-up scratch: %s", cudaGetErrorString(e)));
 
   StepArgs &a = h->args;
   a.p = h->dp;
@@ -466,10 +472,13 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   for (int f = 0; f < 3; ++f) a.frame[f] = h->frame_mem + size_t(f) * fcells;
   a.ctrl = h->ctrl;
   a.partials = h->partials;
+  a.fix = h->fix;
   a.nstrips = nstrips;
   a.nblocks = int(blocks);
   a.work = work;
+  a.fix_blocks = fix_blocks;
   FV_CUDA(cudaMemsetAsync(h->state_mem, 0, 6 * h->field_stride * sizeof(float), h->stream));
+  FV_CUDA(cudaMemsetAsync(h->fix, 0, fix_words * sizeof(uint32_t), h->stream));
   s = reset_ctrl(h);
   if (s != FV_OK) return cleanup(s);
   e = cudaStreamSynchronize(h->stream);
@@ -488,6 +497,7 @@ fv_status fv_destroy(fv_handle *h) {
   if (h->ctrl) cudaFree(h->ctrl);
   if (h->ctrl_host) cudaFreeHost(h->ctrl_host);
   if (h->partials) cudaFree(h->partials);
+  if (h->fix) cudaFree(h->fix);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return FV_OK;

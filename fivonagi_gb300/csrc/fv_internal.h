@@ -69,16 +69,40 @@ __host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny
   return 4 * nx + 2 * ny + 2 * j + (i - nx + 2);
 }
 
+// Fix-up bookkeeping of the step kernel. The step kernel divides with
+// FMA-based division and marks the rows whose results may differ from IEEE
+// division; a second kernel recomputes those rows with exact division. Rows
+// are marked in chunks of kFixRows rows of one warp window (the 26 output
+// columns of one warp of a strip). Layout of the uint32 scratch:
+//   [0] number of listed chunks   [1] fix-up work cursor   [2], [3] unused
+//   bitmap of marked chunks (one bit per chunk), then the list of marked
+//   chunk ids (window * chunks_per_window + chunk), one per marked chunk.
+constexpr int kFixRows = 8;
+__host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
+  return (ny + kFixRows - 1) / kFixRows;
+}
+__host__ __device__ __forceinline__ long long fix_bitmap_words(long long windows, int ny) {
+  return (windows * fix_chunks_per_window(ny) + 31) / 32;
+}
+// uint32 words of the whole fix-up scratch for `windows` warp windows
+__host__ __device__ __forceinline__ long long fix_scratch_words(long long windows, int ny) {
+  return 4 + fix_bitmap_words(windows, ny) + windows * fix_chunks_per_window(ny);
+}
+
 struct StepArgs {
   DevParams p;
   float *state[2][3];     // two full state buffers (u1, u2, u3 each)
   float *frame[3];        // ghost frame (see frame_index)
   Ctrl *ctrl;
-  float *partials;        // one CFL maximum per CTA
+  float *partials;        // one CFL maximum per CTA of the step launch, then
+                          // one per CTA of the fix-up launch
   float *dbg[3];          // debug-stage output (stage kernels only)
+  uint32_t *fix;          // fix-up scratch, zero between attempts (see above)
   int32_t nstrips;        // column strips of width kWarpCols * warps
   int32_t nblocks;        // CTAs of the launch
   int64_t work;           // nstrips * ny: strip-rows to share among the CTAs
+  int32_t fix_blocks;     // CTAs of the fix-up launch
+  int32_t pad0;
 };
 
 // One simulation of a batch: its parameters, buffers and control block,

@@ -6,7 +6,7 @@
 // library allocation bypass their accounting, or fail outright once the
 // arena holds the whole device. fv_step_noalloc serves them: the caller
 // passes the input and output state buffers, and the step kernel's scratch
-// (control block, per-CTA CFL maxima, ghost frame) lives in one file-scope
+// (control block, per-CTA CFL maxima, ghost frame, fix-up scratch) lives in one file-scope
 // __device__ array of fixed size instead of fv_create's allocations.
 //
 // The array is FV_NOALLOC_SCRATCH_BYTES per device; every GPU that loads the
@@ -28,12 +28,16 @@ using namespace fvgb;
 namespace {
 
 constexpr int kNoallocMaxCtas = FV_NOALLOC_MAX_CTAS;
+constexpr int kNoallocMaxFixCtas = 1024;                          // CTAs of the fix-up launch
 constexpr int kNoallocMaxFrame = 4 * FV_NOALLOC_MAX_PERIMETER;  // frame_cells(nx, ny) <= this
 constexpr size_t kCtrlBytes = 256;                               // Ctrl, padded
-constexpr size_t kPartialBytes = size_t(kNoallocMaxCtas) * sizeof(float);
+constexpr size_t kPartialBytes = size_t(kNoallocMaxCtas + kNoallocMaxFixCtas) * sizeof(float);
 constexpr size_t kFrameBytes = 3 * size_t(kNoallocMaxFrame) * sizeof(float);
+// fix_scratch_words() of every grid with nx + ny <= 16384 is at most
+// 336633 words (nx = 8120, ny = 8264); the host checks each call's need.
+constexpr size_t kFixBytes = 337920 * sizeof(uint32_t);
 static_assert(sizeof(Ctrl) <= kCtrlBytes, "control block does not fit its slot");
-static_assert(kCtrlBytes + kPartialBytes + kFrameBytes <= FV_NOALLOC_SCRATCH_BYTES,
+static_assert(kCtrlBytes + kPartialBytes + kFrameBytes + kFixBytes <= FV_NOALLOC_SCRATCH_BYTES,
               "scratch layout exceeds FV_NOALLOC_SCRATCH_BYTES");
 
 // The scratch itself: a host-side stand-in in host code, a real array on
@@ -44,6 +48,7 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
 int g_max_resident[kMaxDevices] = {};
+int g_sms[kMaxDevices] = {};
 
 // Errors go to the library's per-thread message (fv_last_error_string).
 fv_status nafail(fv_status s, const char *msg, cudaError_t e = cudaSuccess) {
@@ -57,8 +62,12 @@ fv_status nafail(fv_status s, const char *msg, cudaError_t e = cudaSuccess) {
 }
 
 // Writes every control-block field the step kernel reads or counts with,
-// so the previous call's contents never leak into this one.
-__global__ void noalloc_begin_kernel(Ctrl *c, float dt, float T, int mdx, int mdy, int max_retries) {
+// and zeroes the fix-up counters and bitmap, so the previous call's
+// contents never leak into this one.
+__global__ void noalloc_begin_kernel(Ctrl *c, uint32_t *fix, int fix_zero_words, float dt, float T,
+                                     int mdx, int mdy, int max_retries) {
+  for (int k = threadIdx.x; k < fix_zero_words; k += blockDim.x) fix[k] = 0u;
+  if (threadIdx.x != 0) return;
   c->dt = dt;
   c->T = T;
   c->last_cfl = 0.0f;
@@ -99,7 +108,7 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   if (e != cudaSuccess) return nafail(FV_NO_DEVICE, "cudaGetDevice", e);
   if (dev < 0 || dev >= kMaxDevices) return nafail(FV_NO_DEVICE, "device index out of range");
   unsigned char *base = nullptr;
-  int max_resident = 0;
+  int max_resident = 0, sms = 0;
   {
     // Set-up, once per device, with that device current.
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -113,10 +122,12 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
       if (e != cudaSuccess || !ptr) return nafail(FV_CUDA_ERROR, "cudaGetSymbolAddress(scratch)", e);
       const int per_sm = p->exact ? max_blocks_per_sm_exact(4, -1) : max_blocks_per_sm_fast(4, -1);
       g_max_resident[dev] = per_sm * prop.multiProcessorCount;
+      g_sms[dev] = prop.multiProcessorCount;
       g_scratch_addr[dev] = static_cast<unsigned char *>(ptr);
     }
     base = g_scratch_addr[dev];
     max_resident = g_max_resident[dev];
+    sms = g_sms[dev];
   }
 
   StepArgs a{};
@@ -126,9 +137,13 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   const long long work = (long long)nstrips * p->ny;
   long long blocks = std::max(1LL, std::min(4LL * max_resident, work / 32));
   if (blocks > kNoallocMaxCtas) blocks = kNoallocMaxCtas;
+  const long long windows = (long long)nstrips * 4;
+  if (size_t(fix_scratch_words(windows, p->ny)) * sizeof(uint32_t) > kFixBytes)
+    return nafail(FV_BAD_ARG, "grid needs more fix-up scratch than the scratch array holds");
   Ctrl *ctrl = reinterpret_cast<Ctrl *>(base);
   float *partials = reinterpret_cast<float *>(base + kCtrlBytes);
   float *frame = reinterpret_cast<float *>(base + kCtrlBytes + kPartialBytes);
+  uint32_t *fix = reinterpret_cast<uint32_t *>(base + kCtrlBytes + kPartialBytes + kFrameBytes);
   const size_t fcells = size_t(frame_cells(p->nx, p->ny));
   a.state[0][0] = const_cast<float *>(in_u1);
   a.state[0][1] = const_cast<float *>(in_u2);
@@ -139,12 +154,16 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   for (int f = 0; f < 3; ++f) a.frame[f] = frame + size_t(f) * fcells;
   a.ctrl = ctrl;
   a.partials = partials;
+  a.fix = fix;
   a.nstrips = nstrips;
   a.nblocks = int(blocks);
   a.work = work;
+  a.fix_blocks = std::min(kNoallocMaxFixCtas, std::max(1, 4 * sms));
 
   cudaStream_t st = (cudaStream_t)cuda_stream;
-  noalloc_begin_kernel<<<1, 1, 0, st>>>(ctrl, float(dt), float(T), mdx, mdy, a.p.max_retries);
+  const int fix_zero_words = int(4 + fix_bitmap_words(windows, p->ny));
+  noalloc_begin_kernel<<<1, 256, 0, st>>>(ctrl, fix, fix_zero_words, float(dt), float(T), mdx, mdy,
+                                          a.p.max_retries);
   e = cudaGetLastError();
   if (e != cudaSuccess) return nafail(FV_CUDA_ERROR, "control-block launch", e);
   const int rc = p->exact ? launch_step_exact(a, 4, -1, st) : launch_step_fast(a, 4, -1, st);

@@ -31,10 +31,23 @@
 // (column strip, row) space, so every CTA streams the same number of rows;
 // a share may span two strips.
 //
+// Division: the step kernel divides with Markstein's FMA sequence
+// (DivFma, fv_device.cuh), which equals IEEE division unless an operand is
+// tiny, huge or not finite. A warp that meets such an operand in an
+// iteration marks the rows that iteration can influence (chunks of
+// kFixRows rows of its window) and leaves their CFL and negative-eigenvalue
+// checks out; a fix-up kernel then recomputes the marked chunks from the
+// same input with exact division (IEEE division wherever FMA division's
+// conditions fail), overwriting their output, and its last CTA accepts or
+// rejects the attempt. Marked chunks are rare (the decaying
+// tails of a wave front), and the step kernel itself stays branch-free.
+//
 // This file is compiled twice: FV_VARIANT_EXACT with --fmad=false (the
 // oracle's evaluation, bit for bit) and the fast variant with FMA
 // contraction.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "fv_device.cuh"
 
@@ -60,11 +73,66 @@ struct Cell3 {
   float u1, u2, u3;
 };
 
+// Results of the y chain of one iteration (interface r, flux r-1).
+struct YOut {
+  float vx, vy;  // velocities of row r
+  WaveN w;       // waves at interface r
+  Fluct f;
+  float cy;      // CFL of interface r
+  bool ok;       // no negative eigenvalue
+  Dots dr;       // dots of interfaces r-1, r
+  float fa1, fa2, fa3;  // correction flux at interface r-1
+};
+
+// Results of the x chain of one iteration (row r-3).
+struct XOut {
+  Cell3 s2;        // state after the x sweep
+  float vx2, vy2;  // its velocities
+  float cx;        // CFL of the cell (y and x interfaces)
+  bool ok;
+};
+
 __device__ __forceinline__ void store3(float *const *out, int o, const Cell3 &v) {
   out[0][o] = v.u1;
   out[1][o] = v.u2;
   out[2][o] = v.u3;
 }
+
+// Marks chunks of one warp window for the fix-up kernel (layout in
+// fv_internal.h). Called warp-uniformly; lane 0 does the atomics. The
+// layout is read from the launch's parameters when a mark happens, so the
+// row loop holds only `last` in a register.
+struct StepMarker {
+  const StepArgs &a;
+  int last;  // last chunk this warp marked in this strip segment
+  // rows lo..hi (inclusive) of the window of the warp at column xw
+  __device__ __forceinline__ void mark(int xw, int lo, int hi) {
+    const int c0 = max(lo / kFixRows, last + 1), c1 = hi / kFixRows;
+    if ((threadIdx.x & 31) == 0) {
+      const unsigned cpw = (unsigned)fix_chunks_per_window(a.p.ny);
+      const unsigned words = (unsigned)fix_bitmap_words((long long)a.nstrips * (kStripCols / kWarpCols), a.p.ny);
+      uint32_t *fix = a.fix;
+      for (int c = c0; c <= c1; ++c) {
+        const unsigned id = (unsigned)(xw / kWarpCols) * cpw + (unsigned)c;
+        const unsigned bit = 1u << (id & 31u);
+        if (!(atomicOr(fix + 4 + (id >> 5), bit) & bit)) fix[4 + words + atomicAdd(fix, 1u)] = id;
+      }
+    }
+    last = max(last, c1);
+  }
+};
+
+// For division policies that never flag.
+struct NoMarker {
+  __device__ __forceinline__ void mark(int, int, int) {}
+};
+
+// Records that some iteration was flagged (the fix-up pass redoes the
+// window with IEEE division then).
+struct FlagMarker {
+  bool flagged = false;
+  __device__ __forceinline__ void mark(int, int, int) { flagged = true; }
+};
 
 // Stream one warp's 32 columns over output rows [y0, y1) of a strip.
 //
@@ -79,12 +147,24 @@ __device__ __forceinline__ void store3(float *const *out, int o, const Cell3 &v)
 // loop body free of branches.
 // EDGE: the warp's columns include ghost columns.
 // STAGE < 0: full step into `out`; STAGE 0..3: that stage's grid into `out`.
-template <int STAGE, bool EDGE>
+// DP: division policy. With DivFma, an iteration whose divisions may differ
+// from IEEE division marks the output rows it can influence (mk), and the
+// CFL and negative-eigenvalue checks that depend on it are left to the
+// fix-up kernel:
+//   a division of the y chain of iteration f (row f's velocities, the
+//   interface f solve, the limiter at f-1) feeds the waves at interfaces f
+//   and f+1, hence the correction fluxes at f-1 .. f+2, the y-updated rows
+//   f-2 .. f+2, and after diffusion rows f-3 .. f+3; the x chain of
+//   iteration f (row f-3) feeds diffusion rows f-4 .. f-2. So iteration f
+//   marks rows f-4 .. f+3. The CFL of row r-3, taken in iteration r,
+//   depends on y chains r-5 .. r-1 and the x chain r; the y solve's
+//   eigenvalue check at interface r on y chains r-1 and r.
+template <int STAGE, bool EDGE, class DP, class MK>
 __device__ __forceinline__ void stream_strip(const DevParams &p, const float *const *in,
                                              const float *const *frame,
                                              float *const *out, int xw, int y0, int y1,
                                              float dt, float T, int mdx, int mdy, int shx,
-                                             int shy, float &cmax, bool &neg) {
+                                             int shy, float &cmax, bool &neg, MK &mk) {
   const int lane = threadIdx.x & (kLanes - 1);
   const int nx = p.nx, ny = p.ny;
   const int i = xw - kHalo + lane;
@@ -132,6 +212,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   load_raw(y0 - 3, pf0);
   load_raw(y0 - 2, pf1);
 
+  unsigned yhist = 0u;
   const int r_end = y1 + 4;
   for (int r = y0 - 3; r <= r_end; ++r) {
     Cell3 u = pf0;
@@ -139,20 +220,72 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     if (r + 2 <= y1 + 2) load_raw(r + 2, pf1);
 
     // ======== Y chain: interface r, flux r-1, update of row r-2
-    const float rho = u.u1 + 1.0f;
-    const float vx = fdiv(u.u2, rho);
-    const float vy = fdiv(u.u3, rho);
-    WaveN w;
-    Fluct f;
-    float cy = 0.0f;
-    const bool oky = riemann(rho, u.u3, u.u2, vy, vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
-                             vx_m1, two_bm1, dty, cy, w, f);
-    cy = (r <= 0) ? 0.0f : cy;  // cfl = 0 on j == 0 (apps/na/fv.h:212-215)
-    neg = neg || (!oky && out_lane && r >= y0 && r < y1 && r >= 1);
-    const float fn1 = ap1 + f.am1, fn2 = ap2 + f.am2, fn3 = ap3 + f.am3;
-    const Dots dr = wave_dots(w_m1, w);
-    float fan1, fan2, fan3;
-    correction(w_m1, dl_m1, dr, dty, fan1, fan2, fan3);
+    // ======== X chain: row r-3; normal = u2, transverse = u3
+    YOut yo;
+    XOut xo;
+    auto y_chain = [&](auto &dp) {
+      const float rho = u.u1 + 1.0f;
+      const auto rr = dp.recip(rho);
+      yo.vx = dp.div_r(u.u2, rr);
+      yo.vy = dp.div_r(u.u3, rr);
+      yo.cy = 0.0f;
+      yo.ok = riemann(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
+                      vx_m1, two_bm1, dty, yo.cy, yo.w, yo.f, dp);
+      yo.dr = wave_dots(w_m1, yo.w);
+      correction(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp);
+    };
+    auto x_chain = [&](auto &dp) {
+      const float rho1 = s1_m3.u1 + 1.0f;
+      const auto rr = dp.recip(rho1);
+      const float vn1 = dp.div_r(s1_m3.u2, rr);
+      const float vt1 = dp.div_r(s1_m3.u3, rr);
+      const float rho1m = shup(rho1), u2m = shup(s1_m3.u2), u3m = shup(s1_m3.u3);
+      const float vn1m = shup(vn1), vt1m = shup(vt1);
+      WaveN wx;
+      Fluct fx;
+      xo.cx = cy_m3;  // the x kernel starts from the cell's y value (fv.h:57)
+      xo.ok = riemann(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m, two_bm1,
+                      dtx, xo.cx, wx, fx, dp);
+      WaveN wn;
+      wn.w11 = shdn(wx.w11); wn.w21 = shdn(wx.w21); wn.w31 = shdn(wx.w31);
+      wn.w12 = shdn(wx.w12); wn.w22 = shdn(wx.w22); wn.w32 = shdn(wx.w32);
+      wn.w33 = shdn(wx.w33);
+      const Dots drx = wave_dots(wx, wn);
+      Dots dlx;
+      dlx.d1 = shup(drx.d1); dlx.d2 = shup(drx.d2); dlx.d3 = shup(drx.d3);
+      float fx1, fx2, fx3;
+      correction(wx, dlx, drx, dtx, fx1, fx2, fx3, dp);
+      const float amn1 = shdn(fx.am1), amn2 = shdn(fx.am2), amn3 = shdn(fx.am3);
+      const float fxn1 = shdn(fx1), fxn2 = shdn(fx2), fxn3 = shdn(fx3);
+      const bool in_x = col_int && r - 3 >= 2 && r - 3 <= ny - 3;
+      const float m1 = s1_m3.u1 - dtx * (fx.ap1 + amn1);
+      const float m2 = s1_m3.u2 - dtx * (fx.ap2 + amn2);
+      const float m3 = s1_m3.u3 - dtx * (fx.ap3 + amn3);
+      xo.s2.u1 = in_x ? m1 - dtx * (fxn1 - fx1) : s1_m3.u1;
+      xo.s2.u2 = in_x ? m2 - dtx * (fxn2 - fx2) : s1_m3.u2;
+      xo.s2.u3 = in_x ? m3 - dtx * (fxn3 - fx3) : s1_m3.u3;
+      const float rho2 = xo.s2.u1 + 1.0f;
+      const auto rr2 = dp.recip(rho2);
+      xo.vx2 = dp.div_r(xo.s2.u2, rr2);
+      xo.vy2 = dp.div_r(xo.s2.u3, rr2);
+    };
+    DP dy, dx;
+    y_chain(dy);
+    x_chain(dx);
+    bool excl_y = false, excl_x = false, flagged = false;
+    if constexpr (DP::kFlags) {
+      const bool yf = __any_sync(0xffffffffu, dy.unsafe());
+      const bool xf = __any_sync(0xffffffffu, dx.unsafe());
+      yhist = (yhist << 1) | (yf ? 1u : 0u);  // bit k: y chain of iteration r-k
+      excl_y = (yhist & 0x3u) != 0u;
+      excl_x = xf || (yhist & 0x3eu) != 0u;
+      flagged = yf || xf;
+    }
+
+    // ---- Y results
+    const float cy = (r <= 0) ? 0.0f : yo.cy;  // cfl = 0 on j == 0 (apps/na/fv.h:212-215)
+    neg = neg || (!yo.ok && !excl_y && out_lane && r >= y0 && r < y1 && r >= 1);
+    const float fn1 = ap1 + yo.f.am1, fn2 = ap2 + yo.f.am2, fn3 = ap3 + yo.f.am3;
     const int cyr = r - 2;  // row of the y update
     Cell3 s1 = s0_m2;
     {
@@ -161,60 +294,26 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       const float m3 = s0_m2.u3 - dty * fo2;
       const float m2 = s0_m2.u2 - dty * fo3;
       const bool in_y = col_int && cyr >= 2 && cyr <= ny - 3;
-      s1.u1 = in_y ? m1 - dty * (fan1 - fa1) : s0_m2.u1;
-      s1.u3 = in_y ? m3 - dty * (fan2 - fa2) : s0_m2.u3;
-      s1.u2 = in_y ? m2 - dty * (fan3 - fa3) : s0_m2.u2;
+      s1.u1 = in_y ? m1 - dty * (yo.fa1 - fa1) : s0_m2.u1;
+      s1.u3 = in_y ? m3 - dty * (yo.fa2 - fa2) : s0_m2.u3;
+      s1.u2 = in_y ? m2 - dty * (yo.fa3 - fa3) : s0_m2.u2;
     }
     if (STAGE == FV_STAGE_BOUNDARY || STAGE == FV_STAGE_SWEEP_Y) {
       if (out_lane && cyr >= y0 && cyr < y1) store3(out, i + cyr * nx, STAGE == FV_STAGE_BOUNDARY ? s0_m2 : s1);
     }
 
-    // ======== X chain: row r-3; normal = u2, transverse = u3
+    // ---- X results
     const int cxr = r - 3;
-    const float rho1 = s1_m3.u1 + 1.0f;
-    const float vn1 = fdiv(s1_m3.u2, rho1);
-    const float vt1 = fdiv(s1_m3.u3, rho1);
-    const float rho1m = shup(rho1), u2m = shup(s1_m3.u2), u3m = shup(s1_m3.u3);
-    const float vn1m = shup(vn1), vt1m = shup(vt1);
-    WaveN wx;
-    Fluct fx;
-    float cx = cy_m3;  // the x kernel starts from the cell's y value (fv.h:57)
-    const bool okx = riemann(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m,
-                             two_bm1, dtx, cx, wx, fx);
     const bool own_x = out_lane && cxr >= y0 && cxr < y1;
-    neg = neg || (!okx && own_x && i >= 1);
-    WaveN wn;
-    wn.w11 = shdn(wx.w11); wn.w21 = shdn(wx.w21); wn.w31 = shdn(wx.w31);
-    wn.w12 = shdn(wx.w12); wn.w22 = shdn(wx.w22); wn.w32 = shdn(wx.w32);
-    wn.w33 = shdn(wx.w33);
-    const Dots drx = wave_dots(wx, wn);
-    Dots dlx;
-    dlx.d1 = shup(drx.d1); dlx.d2 = shup(drx.d2); dlx.d3 = shup(drx.d3);
-    float fx1, fx2, fx3;
-    correction(wx, dlx, drx, dtx, fx1, fx2, fx3);
-    const float amn1 = shdn(fx.am1), amn2 = shdn(fx.am2), amn3 = shdn(fx.am3);
-    const float fxn1 = shdn(fx1), fxn2 = shdn(fx2), fxn3 = shdn(fx3);
-    Cell3 s2;
-    {
-      const bool in_x = col_int && cxr >= 2 && cxr <= ny - 3;
-      const float m1 = s1_m3.u1 - dtx * (fx.ap1 + amn1);
-      const float m2 = s1_m3.u2 - dtx * (fx.ap2 + amn2);
-      const float m3 = s1_m3.u3 - dtx * (fx.ap3 + amn3);
-      s2.u1 = in_x ? m1 - dtx * (fxn1 - fx1) : s1_m3.u1;
-      s2.u2 = in_x ? m2 - dtx * (fxn2 - fx2) : s1_m3.u2;
-      s2.u3 = in_x ? m3 - dtx * (fxn3 - fx3) : s1_m3.u3;
-    }
-    const float rho2 = s2.u1 + 1.0f;
-    const float vx2 = fdiv(s2.u2, rho2);
-    const float vy2 = fdiv(s2.u3, rho2);
+    neg = neg || (!xo.ok && !excl_x && own_x && i >= 1);
     {
       // CFL of cell (i, r-3): its y and x interfaces; 0 on i == 0
-      const float cell = (i == 0) ? 0.0f : cx;
-      const bool counted = own_x && (!even_only || ((i + cxr * nx) & 1) == 0);
+      const float cell = (i == 0) ? 0.0f : xo.cx;
+      const bool counted = own_x && !excl_x && (!even_only || ((i + cxr * nx) & 1) == 0);
       cmax = counted ? nanmax(cmax, cell) : cmax;
     }
     if (STAGE == FV_STAGE_SWEEP_X) {
-      if (own_x) store3(out, i + cxr * nx, s2);
+      if (own_x) store3(out, i + cxr * nx, xo.s2);
     }
 
     // ======== D chain: diffusion of row r-5 (apps/na/source.h:22-104)
@@ -248,22 +347,30 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     // ======== rotate
     s0_m2 = s0_m1;
     s0_m1 = u;
-    vx_m1 = vx;
-    vy_m1 = vy;
-    w_m1 = w;
-    dl_m1 = dr;
-    ap1 = f.ap1; ap2 = f.ap2; ap3 = f.ap3;
+    vx_m1 = yo.vx;
+    vy_m1 = yo.vy;
+    w_m1 = yo.w;
+    dl_m1 = yo.dr;
+    ap1 = yo.f.ap1; ap2 = yo.f.ap2; ap3 = yo.f.ap3;
     fo1 = fn1; fo2 = fn2; fo3 = fn3;
-    fa1 = fan1; fa2 = fan2; fa3 = fan3;
+    fa1 = yo.fa1; fa2 = yo.fa2; fa3 = yo.fa3;
     cy_m3 = cy_m2;
     cy_m2 = cy_m1;
     cy_m1 = cy;
     s1_m3 = s1;
     s2_m5 = s2_m4;
-    s2_m4 = s2;
+    s2_m4 = xo.s2;
     vx2_m6 = vx2_m5; vy2_m6 = vy2_m5;
     vx2_m5 = vx2_m4; vy2_m5 = vy2_m4;
-    vx2_m4 = vx2; vy2_m4 = vy2;
+    vx2_m4 = xo.vx2; vy2_m4 = xo.vy2;
+
+    // ======== rare: mark the rows this iteration can influence
+    if constexpr (DP::kFlags) {
+      if (flagged) {
+        const int lo = max(r - 4, y0), hi = min(r + 3, y1 - 1);
+        if (lo <= hi) mk.mark(xw, lo, hi);
+      }
+    }
   }
 }
 
@@ -319,12 +426,13 @@ __device__ __forceinline__ bool attempt_active(const Ctrl *ctl) {
   return status == 0 && remaining > 0 && T0 < ts;
 }
 
-// Reduce the partial CFL maxima and decide; runs on the last CTA of the
-// launch (all its threads).
+// Reduce the partial CFL maxima of the step and fix-up launches and
+// decide; runs on the last CTA of the fix-up launch (all its threads).
 __device__ void finalize(const StepArgs &a, float *red) {
   Ctrl *ctl = a.ctrl;
   float m = 0.0f;
-  for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x) m = nanmax(m, __ldcg(a.partials + b));
+  const int np = a.nblocks + a.fix_blocks;
+  for (int b = threadIdx.x; b < np; b += blockDim.x) m = nanmax(m, __ldcg(a.partials + b));
   for (int off = 16; off > 0; off >>= 1) m = nanmax(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
@@ -333,37 +441,96 @@ __device__ void finalize(const StepArgs &a, float *red) {
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) cfl = nanmax(cfl, red[w]);
   volatile Ctrl *vc = ctl;
   decide(vc, a.p, cfl, vc->neg_flag != 0);
+  // the fix-up scratch is zero again for the next attempt (the bitmap was
+  // cleared chunk by chunk)
+  volatile uint32_t *fx = a.fix;
+  fx[0] = 0u;
+  fx[1] = 0u;
   __threadfence();
   vc->blocks_done = 0;
 }
 
+// Shift of the moving window this attempt applies if it is accepted:
+// updateMDXY with the updated T (common/main.cu:126-137, 166-177); 0 before
+// MDT.
+__device__ __forceinline__ void window_shift(const DevParams &p, float T, float dt, int mdx, int mdy,
+                                             int &shx, int &shy) {
+  shx = 0;
+  shy = 0;
+  if (p.moving_domain) {
+    const float Tn = T + dt;
+    if (Tn >= p.mdt) {
+      shx = static_cast<int>((Tn - p.mdt) * p.mdvx / p.dx) - mdx;
+      shy = static_cast<int>((Tn - p.mdt) * p.mdvy / p.dy) - mdy;
+    }
+  }
+}
+
+// One warp's window [y0, y1) at column xw, with the division policy DP.
+template <int STAGE, class DP, class MK>
+__device__ __forceinline__ void stream_window(const DevParams &p, const float *const *in,
+                                              const float *const *frame, float *const *out,
+                                              int xw, int y0, int y1, float dt, float T, int mdx,
+                                              int mdy, int shx, int shy, float &cmax, bool &neg,
+                                              MK &mk) {
+  // ghost columns among the warp's 32 columns?
+  const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= p.nx - 2);
+  if (edge)
+    stream_strip<STAGE, true, DP>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+  else
+    stream_strip<STAGE, false, DP>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+}
+
+// The CTA's CFL maximum into partials[slot], and the negative-eigenvalue
+// flag into the control block. With `count`, returns (to every thread)
+// whether this CTA is the last of `nblocks` to get here, counted on the
+// control block's blocks_done.
+__device__ __forceinline__ bool publish(const StepArgs &a, float cmax, bool neg, int slot,
+                                        int nblocks, bool count, float *red, int *sh) {
+  const int warp = threadIdx.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+  if (threadIdx.x == 0) sh[0] = 0;
+  __syncthreads();
+  if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) sh[0] = 1;
+  if ((threadIdx.x & 31) == 0) red[warp] = cmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = red[0];
+    for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
+    a.partials[slot] = m;
+    if (sh[0]) ((volatile Ctrl *)a.ctrl)->neg_flag = 1;
+    sh[1] = 0;
+    if (count) {
+      __threadfence();
+      const unsigned prev = atomicAdd(&a.ctrl->blocks_done, 1u);
+      sh[1] = (prev == (unsigned)(nblocks - 1)) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  return sh[1] != 0;
+}
+
+// The step: STAGE < 0 is the full attempt with FMA division, followed by
+// the fix-up launch; STAGE 0..3 write that stage's grid to the debug
+// buffers with IEEE division.
 template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   __shared__ float red[kWarps];
-  __shared__ int neg_any;
-  __shared__ int is_last;
+  __shared__ int sh[2];
   const Ctrl *ctl = a.ctrl;
   // Uniform early exit: the control block only changes between launches.
   if (STAGE < 0 && !attempt_active(ctl)) return;
-  if (threadIdx.x == 0) neg_any = 0;
-  __syncthreads();
   const float dt = __ldcg(&ctl->dt);
   const float T = __ldcg(&ctl->T);
   const int cur = __ldcg(&ctl->cur);
   const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
-  // Window shift this attempt applies if it is accepted: updateMDXY with the
-  // updated T (common/main.cu:126-137, 166-177); 0 before MDT.
   int shx = 0, shy = 0;
-  if (STAGE < 0 && a.p.moving_domain) {
-    const float Tn = T + dt;
-    if (Tn >= a.p.mdt) {
-      shx = static_cast<int>((Tn - a.p.mdt) * a.p.mdvx / a.p.dx) - mdx;
-      shy = static_cast<int>((Tn - a.p.mdt) * a.p.mdvy / a.p.dy) - mdy;
-    }
-  }
+  if (STAGE < 0) window_shift(a.p, T, dt, mdx, mdy, shx, shy);
   const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
   float *out[3];
   for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
+  const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
+  using DP = typename std::conditional<(STAGE < 0), DivFma, DivIEEE>::type;
 
   const int warp = threadIdx.x >> 5;
   const int ny = a.p.ny;
@@ -379,34 +546,80 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     const int y1 = (int)((long long)y0 + left < ny ? (long long)y0 + left : ny);
     const int xw = strip * kStripCols + warp * kWarpCols;
     if (xw < a.p.nx) {
-      // ghost columns among the warp's 32 columns?
-      const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= a.p.nx - 2);
-      const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
-      if (edge)
-        stream_strip<STAGE, true>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
-      else
-        stream_strip<STAGE, false>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
+      if constexpr (STAGE < 0) {
+        StepMarker mk{a, -1};
+        stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+      } else {
+        NoMarker mk;
+        stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+      }
     }
     pos += y1 - y0;
   }
   if (STAGE >= 0) return;
+  publish(a, cmax, neg, blockIdx.x, a.nblocks, false, red, sh);
+}
 
-  // CTA maximum of the CFL, and the negative-eigenvalue flag
-  for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
-  if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) neg_any = 1;
-  if ((threadIdx.x & 31) == 0) red[warp] = cmax;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float m = red[0];
-    for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
-    a.partials[blockIdx.x] = m;
-    if (neg_any) ((volatile Ctrl *)a.ctrl)->neg_flag = 1;
-    __threadfence();
-    const unsigned prev = atomicAdd(&a.ctrl->blocks_done, 1u);
-    is_last = (prev == (unsigned)(a.nblocks - 1));
+// Recomputes the chunks the step launch marked, with exact division
+// (DivExact), then decides the attempt on its last CTA. Each chunk is split
+// into items of kFixItemRows rows; warps take items from a shared cursor.
+// The rows of an item are a serial loop (plus the pipeline's 8 rows of
+// warm-up and drain) that runs with few other warps on its SM, so its
+// latency, not the work, sets the pass's duration: short items keep it
+// small. An item whose operands fall outside DivExact's range (never in a
+// physical state) is redone with IEEE division.
+constexpr int kFixItemRows = 2;
+static_assert(kFixRows % kFixItemRows == 0, "fix-up items must tile a chunk");
+
+__global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
+  __shared__ float red[kWarps];
+  __shared__ int sh[2];
+  const Ctrl *ctl = a.ctrl;
+  if (!attempt_active(ctl)) return;
+  const float dt = __ldcg(&ctl->dt);
+  const float T = __ldcg(&ctl->T);
+  const int cur = __ldcg(&ctl->cur);
+  const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
+  int shx = 0, shy = 0;
+  window_shift(a.p, T, dt, mdx, mdy, shx, shy);
+  const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
+  float *out[3] = {a.state[cur ^ 1][0], a.state[cur ^ 1][1], a.state[cur ^ 1][2]};
+  const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
+  const int lane = threadIdx.x & 31;
+  const int ny = a.p.ny;
+  const int cpw = fix_chunks_per_window(ny);
+  const long long bitmap_words = fix_bitmap_words((long long)a.nstrips * kWarps, ny);
+  const uint32_t *list = a.fix + 4 + bitmap_words;
+  constexpr unsigned kItems = kFixRows / kFixItemRows;  // items per chunk
+  const unsigned n = __ldcg(a.fix) * kItems;
+  float cmax = 0.0f;
+  bool neg = false;
+  for (;;) {
+    unsigned k = n;
+    if (lane == 0 && n > 0u) k = atomicAdd(a.fix + 1, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= n) break;
+    const unsigned id = __ldcg(list + k / kItems);
+    const int window = (int)(id / (unsigned)cpw), c = (int)(id - (unsigned)window * (unsigned)cpw);
+    if (lane == 0 && k % kItems == 0u) atomicAnd(a.fix + 4 + (id >> 5), ~(1u << (id & 31u)));
+    const int xw = window * kWarpCols;  // strip * kStripCols + warp * kWarpCols
+    const int y0 = c * kFixRows + (int)(k % kItems) * kFixItemRows;
+    if (y0 >= ny) continue;
+    const int y1 = min(ny, y0 + kFixItemRows);
+    float cm = 0.0f;
+    bool ng = false;
+    FlagMarker fm;
+    stream_window<-1, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    if (__any_sync(0xffffffffu, fm.flagged)) {
+      cm = 0.0f;
+      ng = false;
+      NoMarker none;
+      stream_window<-1, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+    }
+    cmax = nanmax(cmax, cm);
+    neg = neg || ng;
   }
-  __syncthreads();
-  if (is_last) {
+  if (publish(a, cmax, neg, a.nblocks + blockIdx.x, a.fix_blocks, true, red, sh)) {
     __threadfence();
     finalize(a, red);
   }
@@ -523,11 +736,8 @@ __global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
         const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
         const int xw = strip * kStripCols + warp * kWarpCols;
         if (xw < p.nx) {
-          const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= p.nx - 2);
-          if (edge)
-            stream_strip<-1, true>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
-          else
-            stream_strip<-1, false>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg);
+          NoMarker none;
+          stream_window<-1, DivIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, none);
         }
         q += y1 - y0;
       }
@@ -582,7 +792,10 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
   ghost_frame_kernel<<<(ftotal + 255) / 256, 256, 0, st>>>(a, stage < 0 ? 1 : 0);
   dim3 grid(a.nblocks), block(kThreads);
   switch (stage) {
-    case -1: step_kernel<-1><<<grid, block, 0, st>>>(a); break;
+    case -1:
+      step_kernel<-1><<<grid, block, 0, st>>>(a);
+      fixup_kernel<<<a.fix_blocks, block, 0, st>>>(a);
+      break;
     case 0: step_kernel<0><<<grid, block, 0, st>>>(a); break;
     case 1: step_kernel<1><<<grid, block, 0, st>>>(a); break;
     case 2: step_kernel<2><<<grid, block, 0, st>>>(a); break;

@@ -222,7 +222,7 @@ fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_residen
  * caller's input state into the caller's output state (NX*NY device floats
  * per field each) at time T with step dt and window offsets mdx, mdy, and
  * allocates nothing: the step kernel's scratch (control block, per-CTA CFL
- * maxima, ghost frame) is one fixed __device__ array of
+ * maxima, ghost frame, fix-up scratch) is one fixed __device__ array of
  * FV_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * the process exits. Limit: nx + ny <= FV_NOALLOC_MAX_PERIMETER; larger grids
  * are rejected with FV_BAD_ARG. All calls on a device share the array, so
@@ -230,7 +230,7 @@ fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_residen
  * each device looks up the array's address, so make it before any stream
  * capture. res->accepted = 0 means CFL >= CFLMAX: retry from the same input
  * with res->dt_next. No reference counterpart. */
-#define FV_NOALLOC_SCRATCH_BYTES (800u * 1024u)
+#define FV_NOALLOC_SCRATCH_BYTES (2104u * 1024u)
 #define FV_NOALLOC_MAX_CTAS 2048
 #define FV_NOALLOC_MAX_PERIMETER 16384
 
