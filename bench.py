@@ -351,7 +351,8 @@ def run_gpu(args):
         },
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": accepted + int(st["rejected"]) + 1,
+        # per attempt: ghost-frame pre-pass, step kernel, fix-up kernel
+        "gpu_launches": 3 * (accepted + int(st["rejected"])),
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
@@ -360,6 +361,86 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line))
+    return 0
+
+
+def run_batched(args):
+    """Config 3: n focused-beam simulations of uneven sizes and physics,
+    stepped by the batched launch, against the same simulations run one at a
+    time with the plain path. Both legs are device-timed with CUDA events."""
+    import torch
+
+    from fivonagi_gb300 import Batch, Simulation, autotune, configs
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    plist = configs.batched(args.instances, seed=args.seed, exact=0 if args.fast else 1)
+    cells = [p.nx * p.ny for p in plist]
+    steps = args.steps
+    stream = torch.cuda.Stream()
+
+    # ---- batched: one launch per attempt of every simulation
+    b = Batch(plist)
+    b.set_stream(stream.cuda_stream)
+    b.init_state()
+    b.run(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.launch_attempts(steps)
+    e1.record(stream)
+    stream.synchronize()
+    clocks = sampler.stop()
+    st = b.sync()
+    ms_batch = e0.elapsed_time(e1)
+    acc = [s["accepted"] for s in st]
+    b.close()
+    batched_rate = sum(c * a for c, a in zip(cells, acc)) / (ms_batch * 1e-3) / 1e9
+
+    # ---- sequential: each simulation alone with the plain path, same steps
+    ms_seq = 0.0
+    acc_seq = 0
+    for p in plist:
+        sim = Simulation(p)
+        sim.set_launch(autotune.tune(p, steps=20))
+        sim.set_stream(stream.cuda_stream)
+        sim.init_state()
+        sim.run(max(args.warmup, 3))
+        e0.record(stream)
+        sim.launch_attempts(steps)
+        e1.record(stream)
+        stream.synchronize()
+        s1 = sim.sync()
+        ms_seq += e0.elapsed_time(e1)
+        acc_seq += p.nx * p.ny * s1["accepted"]
+        sim.close()
+    seq_rate = acc_seq / (ms_seq * 1e-3) / 1e9
+    line = {
+        "metric": "Gcell-updates/s (batched, aggregate)",
+        "value": batched_rate,
+        "unit": "Gcell-updates/s",
+        "n_gpus": 1,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_batch / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{len(plist)} focused-beam simulations, sides from {list(configs.SIDES)}, "
+                               f"seed {args.seed}", "cells_per_step": sum(cells),
+                   "variant": "fast (FMA)" if args.fast else "exact"},
+        "sequential_plain_path": {"value": seq_rate, "unit": "Gcell-updates/s", "ms_total": ms_seq},
+        "batched_over_sequential": batched_rate / seq_rate,
+        "clocks": clocks,
+        # per attempt: ghost-frame pre-pass, batch step kernel, batch fix-up kernel
+        "gpu_launches": 3 * steps,
+    }
+    print(json.dumps(line))
     return 0
 
 
@@ -373,11 +454,17 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU-baseline leg")
+    ap.add_argument("--workload", choices=["plain", "batched"], default="plain",
+                    help="plain: focused beam 4096x2048; batched: config-3 batch vs sequential")
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_gpu(args)
 
 

@@ -66,7 +66,7 @@ struct fv_batch {
   Ctrl *ctrl_host = nullptr;
   uint32_t *cfl_bits = nullptr;
   int32_t *neg = nullptr;
-  unsigned long long *done = nullptr;
+  uint32_t *fix = nullptr;  // fix-up scratch of the batch launches
   float *mem = nullptr;  // all state buffers and frames
   cudaStream_t own_stream = nullptr, stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -179,12 +179,11 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
   if (e == cudaSuccess) e = cudaMalloc(&b->inst, sizeof(BatchInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->cfl_bits, sizeof(uint32_t) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->neg, sizeof(int32_t) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->done, sizeof(unsigned long long) * n);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cleanup(bfail(FV_CUDA_ERROR, "batch allocation: %s", cudaGetErrorString(e)));
   b->stream = b->own_stream;
 
-  long long work = 0;
+  long long work = 0, fix_chunks = 0;
   int max_frame = 0;
   b->host_inst.resize(n);
   for (int k = 0; k < n; ++k) {
@@ -199,12 +198,18 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
     I.work_begin = work;
     I.work = (long long)nstrips * params[k].ny;
     work += I.work;
+    I.fix_base = fix_chunks;
+    fix_chunks += (long long)nstrips * (strip_cols() / kWarpCols) * fix_chunks_per_window(params[k].ny);
     max_frame = std::max(max_frame, 4 * params[k].nx + 4 * (params[k].ny - 4));
   }
+  if (fix_chunks >= (1LL << 32)) return cleanup(bfail(FV_BAD_ARG, "batch above 2^32 fix-up chunks"));
+  const size_t fix_words = size_t(4 + (fix_chunks + 31) / 32 + 2 * fix_chunks);
+  e = cudaMalloc(&b->fix, fix_words * sizeof(uint32_t));
+  if (e != cudaSuccess) return cleanup(bfail(FV_CUDA_ERROR, "cudaMalloc batch fix-up scratch: %s", cudaGetErrorString(e)));
+  FVB_CUDA(cudaMemsetAsync(b->fix, 0, fix_words * sizeof(uint32_t), b->stream));
   FVB_CUDA(cudaMemcpyAsync(b->inst, b->host_inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice, b->stream));
   FVB_CUDA(cudaMemsetAsync(b->cfl_bits, 0, sizeof(uint32_t) * n, b->stream));
   FVB_CUDA(cudaMemsetAsync(b->neg, 0, sizeof(int32_t) * n, b->stream));
-  FVB_CUDA(cudaMemsetAsync(b->done, 0, sizeof(unsigned long long) * n, b->stream));
   FVB_CUDA(cudaMemsetAsync(b->mem, 0, total * sizeof(float), b->stream));
   const int per_sm = exact ? max_batch_blocks_per_sm_exact() : max_batch_blocks_per_sm_fast();
   b->max_resident = per_sm * prop.multiProcessorCount;
@@ -212,10 +217,13 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
   a.inst = b->inst;
   a.cfl_bits = b->cfl_bits;
   a.neg = b->neg;
-  a.done = b->done;
+  a.fix = b->fix;
   a.n = n;
   a.work = work;
+  a.fix_chunks = fix_chunks;
   a.max_frame = max_frame;
+  // the fix-up launch: four CTAs per SM (its occupancy) take the marked chunks
+  a.fix_blocks = 4 * prop.multiProcessorCount;
   a.nblocks = int(std::max(1LL, std::min(4LL * b->max_resident, work / 32)));
   fv_status s = reset_all(b);
   if (s != FV_OK) return cleanup(s);
@@ -233,7 +241,7 @@ fv_status fv_batch_destroy(fv_batch *b) {
   if (b->inst) cudaFree(b->inst);
   if (b->cfl_bits) cudaFree(b->cfl_bits);
   if (b->neg) cudaFree(b->neg);
-  if (b->done) cudaFree(b->done);
+  if (b->fix) cudaFree(b->fix);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
   return FV_OK;

@@ -114,17 +114,23 @@ struct BatchInst {
   Ctrl *ctrl;
   int64_t work_begin;     // first strip-row of this instance in the batch
   int64_t work;           // nstrips * ny
+  int64_t fix_base;       // first chunk id of this instance in the fix-up scratch
 };
 
+// The batch's fix-up scratch has the layout of a single simulation's
+// (fv_internal.h's fix_* helpers) over the concatenated chunk ids of all
+// instances, except that each list entry is a pair (chunk id, instance).
 struct BatchArgs {
   const BatchInst *inst;  // device array of n instances
   uint32_t *cfl_bits;     // per instance: running max CFL as float bits (non-negative)
   int32_t *neg;           // per instance: a Riemann solve met tmp3 < 0
-  unsigned long long *done;  // per instance: strip-rows finished this attempt
+  uint32_t *fix;          // fix-up scratch, zero between attempts
   int32_t n;
   int32_t nblocks;
   int64_t work;           // total strip-rows
+  int64_t fix_chunks;     // total chunks over all instances
   int32_t max_frame;      // largest frame pre-pass work of an instance
+  int32_t fix_blocks;     // CTAs of the fix-up launch
 };
 
 // Launchers, one translation unit per arithmetic variant:

@@ -685,14 +685,45 @@ __global__ void __launch_bounds__(256) batch_frame_kernel(BatchArgs b) {
     frame_job(p, I.state[cur], I.frame, k, T, mdx, mdy);
 }
 
+// Marks chunks of one warp window of batch instance `inst` (layout of
+// BatchArgs::fix): as StepMarker, with the instance's chunk ids offset by
+// its fix_base and the instance index stored beside each listed id.
+struct BatchMarker {
+  const BatchArgs &b;
+  int inst;
+  int last;
+  __device__ __forceinline__ void mark(int xw, int lo, int hi) {
+    const int c0 = max(lo / kFixRows, last + 1), c1 = hi / kFixRows;
+    if ((threadIdx.x & 31) == 0) {
+      const BatchInst &I = b.inst[inst];
+      const long long cpw = fix_chunks_per_window(I.p.ny);
+      const long long words = (b.fix_chunks + 31) / 32;
+      uint32_t *fix = b.fix;
+      for (int c = c0; c <= c1; ++c) {
+        const unsigned long long id = (unsigned long long)I.fix_base + (unsigned long long)(xw / kWarpCols) * cpw + c;
+        const unsigned bit = 1u << (id & 31u);
+        if (!(atomicOr(fix + 4 + (id >> 5), bit) & bit)) {
+          const unsigned slot = atomicAdd(fix, 1u);
+          fix[4 + words + 2 * (long long)slot] = (uint32_t)id;
+          fix[4 + words + 2 * (long long)slot + 1] = (uint32_t)inst;
+        }
+      }
+    }
+    last = max(last, c1);
+  }
+};
+
 // One attempted step of every active simulation of a batch (uneven grid
 // sizes and parameters) in one launch. CTAs share the batch's concatenated
 // (simulation, strip, row) space evenly. A CTA contributes its rows of one
 // simulation with an atomic max of their CFL (float bits of non-negative
-// values order like unsigned integers, and NaN above all) and an atomic
-// count of finished strip-rows; whoever completes a simulation's count
-// decides that simulation's attempt. No CTA waits on another.
-__global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
+// values order like unsigned integers, and NaN above all) and the
+// negative-eigenvalue flag; rows whose FMA division may differ from IEEE
+// division are marked for the batch fix-up launch, whose last CTA decides
+// every simulation's attempt. No CTA waits on another. Three CTAs per SM:
+// the simulation's buffers and parameters come from global memory, and at
+// four the kernel would spill (measured: three is faster).
+__global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
   __shared__ float red[kWarps];
   __shared__ int neg_any;
   const int warp = threadIdx.x >> 5;
@@ -707,20 +738,14 @@ __global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
     const long long kb = I.work_begin, ke = kb + I.work;
     const long long seg_end = s1 < ke ? s1 : ke;
     if (pos < seg_end && attempt_active(I.ctrl)) {
-      const DevParams p = I.p;
+      const DevParams &p = I.p;  // read in place (L1), not copied into registers
       const Ctrl *ctl = I.ctrl;
       const float dt = __ldcg(&ctl->dt);
       const float T = __ldcg(&ctl->T);
       const int cur = __ldcg(&ctl->cur);
       const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
       int shx = 0, shy = 0;
-      if (p.moving_domain) {
-        const float Tn = T + dt;
-        if (Tn >= p.mdt) {
-          shx = static_cast<int>((Tn - p.mdt) * p.mdvx / p.dx) - mdx;
-          shy = static_cast<int>((Tn - p.mdt) * p.mdvy / p.dy) - mdy;
-        }
-      }
+      window_shift(p, T, dt, mdx, mdy, shx, shy);
       const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
       float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
       const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
@@ -736,8 +761,8 @@ __global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
         const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
         const int xw = strip * kStripCols + warp * kWarpCols;
         if (xw < p.nx) {
-          NoMarker none;
-          stream_window<-1, DivIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, none);
+          BatchMarker mk{b, k, -1};
+          stream_window<-1, DivFma>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
         }
         q += y1 - y0;
       }
@@ -750,17 +775,6 @@ __global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
         for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
         atomicMax(b.cfl_bits + k, __float_as_uint(m));
         if (neg_any) atomicExch(b.neg + k, 1);
-        __threadfence();
-        const unsigned long long rows = (unsigned long long)(seg_end - pos);
-        const unsigned long long prev = atomicAdd(b.done + k, rows);
-        if (prev + rows == (unsigned long long)I.work) {
-          __threadfence();
-          const float cfl = __uint_as_float(atomicExch(b.cfl_bits + k, 0u));
-          const int negative = atomicExch(b.neg + k, 0);
-          b.done[k] = 0ull;
-          decide((volatile Ctrl *)I.ctrl, p, cfl, negative != 0);
-          __threadfence();
-        }
       }
       __syncthreads();
     }
@@ -769,11 +783,95 @@ __global__ void __launch_bounds__(kThreads, 4) batch_step_kernel(BatchArgs b) {
   }
 }
 
+// The batch's fix-up launch: recomputes the marked chunks of every
+// simulation in items of kFixItemRows rows with exact division (as
+// fixup_kernel), folds their CFL and eigenvalue checks into the
+// simulation's atomics, and on its last CTA decides every active
+// simulation's attempt and clears the per-simulation accumulators.
+__global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
+  __shared__ int is_last;
+  const int lane = threadIdx.x & 31;
+  constexpr unsigned kItems = kFixRows / kFixItemRows;
+  const long long words = (b.fix_chunks + 31) / 32;
+  const uint32_t *list = b.fix + 4 + words;
+  const unsigned n = __ldcg(b.fix) * kItems;
+  for (;;) {
+    unsigned k = n;
+    if (lane == 0 && n > 0u) k = atomicAdd(b.fix + 1, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= n) break;
+    const unsigned e = k / kItems;
+    const unsigned id = __ldcg(list + 2 * (long long)e);
+    const int inst = (int)__ldcg(list + 2 * (long long)e + 1);
+    if (lane == 0 && k % kItems == 0u) atomicAnd(b.fix + 4 + (id >> 5), ~(1u << (id & 31u)));
+    const BatchInst &I = b.inst[inst];
+    const DevParams p = I.p;
+    const int cpw = fix_chunks_per_window(p.ny);
+    const long long local = (long long)id - I.fix_base;
+    const int window = (int)(local / cpw), c = (int)(local - (long long)window * cpw);
+    const int xw = window * kWarpCols;
+    const int y0 = c * kFixRows + (int)(k % kItems) * kFixItemRows;
+    if (y0 >= p.ny) continue;
+    const int y1 = min(p.ny, y0 + kFixItemRows);
+    const Ctrl *ctl = I.ctrl;
+    const float dt = __ldcg(&ctl->dt);
+    const float T = __ldcg(&ctl->T);
+    const int cur = __ldcg(&ctl->cur);
+    const int mdx = __ldcg(&ctl->mdx), mdy = __ldcg(&ctl->mdy);
+    int shx = 0, shy = 0;
+    window_shift(p, T, dt, mdx, mdy, shx, shy);
+    const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
+    float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
+    const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
+    float cm = 0.0f;
+    bool ng = false;
+    FlagMarker fm;
+    stream_window<-1, DivExact>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    if (__any_sync(0xffffffffu, fm.flagged)) {
+      cm = 0.0f;
+      ng = false;
+      NoMarker none;
+      stream_window<-1, DivIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+    }
+    for (int off = 16; off > 0; off >>= 1) cm = nanmax(cm, __shfl_xor_sync(0xffffffffu, cm, off));
+    const bool wneg = __any_sync(0xffffffffu, ng);
+    if (lane == 0) {
+      atomicMax(b.cfl_bits + inst, __float_as_uint(cm));
+      if (wneg) atomicExch(b.neg + inst, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(b.fix + 2, 1u);
+    is_last = (prev == (unsigned)(b.fix_blocks - 1)) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int k = threadIdx.x; k < b.n; k += blockDim.x) {
+    const BatchInst &I = b.inst[k];
+    if (!attempt_active(I.ctrl)) continue;
+    const float cfl = __uint_as_float(atomicExch(b.cfl_bits + k, 0u));
+    const int negative = atomicExch(b.neg + k, 0);
+    decide((volatile Ctrl *)I.ctrl, I.p, cfl, negative != 0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t *fx = b.fix;
+    fx[0] = 0u;
+    fx[1] = 0u;
+    fx[2] = 0u;
+    __threadfence();
+  }
+}
+
 static int launch_batch_impl(const BatchArgs &b, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   dim3 fgrid((b.max_frame + 255) / 256, b.n);
   batch_frame_kernel<<<fgrid, 256, 0, st>>>(b);
   batch_step_kernel<<<b.nblocks, kThreads, 0, st>>>(b);
+  batch_fixup_kernel<<<b.fix_blocks, kThreads, 0, st>>>(b);
   return (int)cudaGetLastError();
 }
 
