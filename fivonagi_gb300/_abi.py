@@ -41,11 +41,13 @@ FV_APP_HIFU_BEAM = 0
 FV_APP_TAYLOR_ANGLE_XY = 1
 FV_APP_PLANE_WAVE = 2
 FV_APP_FOCUSED_BEAM = 3
+FV_APP_PHASED_ARRAY = 4
 APP_NAMES = {
     "hifu-beam": FV_APP_HIFU_BEAM,
     "taylor-angle-xy": FV_APP_TAYLOR_ANGLE_XY,
     "plane-wave": FV_APP_PLANE_WAVE,
     "focused-beam": FV_APP_FOCUSED_BEAM,
+    "phased-array": FV_APP_PHASED_ARRAY,
 }
 
 # fv_stage
@@ -64,7 +66,7 @@ class FvParams(C.Structure):
         ("moving_domain", C.c_int32),
         ("exact", C.c_int32),
         ("max_retries", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("array_elems", C.c_int32),
         ("xmax", C.c_double),
         ("ymax", C.c_double),
         ("beta", C.c_double),
@@ -122,6 +124,17 @@ class FvRunStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class FvLossWindow(C.Structure):
+    _fields_ = [
+        ("i0", C.c_int32),
+        ("j0", C.c_int32),
+        ("ni", C.c_int32),
+        ("nj", C.c_int32),
+        ("step_first", C.c_int64),
+        ("step_last", C.c_int64),
+    ]
+
+
 class FvStepResult(C.Structure):
     _fields_ = [
         ("accepted", C.c_int32),
@@ -149,6 +162,18 @@ PROTOTYPES = {
     "fv_get_state": (C.c_int, [_P, _P, _P, _P, C.c_int32]),
     "fv_set_scalars": (C.c_int, [_P, C.c_double, C.c_double, C.c_int32]),
     "fv_get_stats": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_set_array_weights": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32]),
+    "fv_adjoint_create": (C.c_int, [C.POINTER(FvParams), C.POINTER(FvLossWindow), C.c_int64, C.c_int32,
+                                    C.POINTER(_P)]),
+    "fv_adjoint_destroy": (C.c_int, [_P]),
+    "fv_adjoint_set_stream": (C.c_int, [_P, _P]),
+    "fv_adjoint_forward": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "fv_adjoint_backward": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "fv_adjoint_replay": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "fv_adjoint_schedule": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "fv_adjoint_get_state": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "fv_snapshot": (C.c_int, [_P]),
+    "fv_restore": (C.c_int, [_P]),
     "fv_set_stream": (C.c_int, [_P, _P]),
     "fv_run": (C.c_int, [_P, C.c_int64, C.POINTER(FvRunStats)]),
     "fv_run_until": (C.c_int, [_P, C.c_double, C.POINTER(FvRunStats)]),

@@ -100,6 +100,10 @@ struct fv_handle {
   Ctrl *ctrl_host = nullptr;    // pinned mirror for reads
   float *partials = nullptr;
   uint32_t *fix = nullptr;      // fix-up scratch of the step launches
+  float *weights = nullptr;     // phased array: amplitudes then phases (device)
+  float *snap_mem = nullptr;    // fv_snapshot: one state (3 fields)
+  Ctrl *snap_ctrl = nullptr;    // fv_snapshot: the control block
+  int snap_cur = -1;            // buffer the snapshot was taken from; -1: none
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -119,7 +123,7 @@ int launch(fv_handle *h, int stage, const StepArgs &a) {
 
 fv_status validate(const fv_params *p) {
   if (!p) return fail(FV_BAD_ARG, "params is NULL");
-  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM)
+  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_PHASED_ARRAY)
     return fail(FV_BAD_ARG, "unknown app %d", p->app);
   if (p->nx < 8 || p->ny < 8) return fail(FV_BAD_ARG, "grid %dx%d below 8x8", p->nx, p->ny);
   if ((long long)p->nx * (long long)p->ny > (1LL << 30))
@@ -129,8 +133,13 @@ fv_status validate(const fv_params *p) {
     return fail(FV_BAD_ARG, "cflmax, cflwhish and dtini must be positive");
   if (p->moving_domain && (p->mdvx < 0 || p->mdvy < 0))
     return fail(FV_BAD_ARG, "moving_domain needs mdvx, mdvy >= 0");
-  if (p->app == FV_APP_FOCUSED_BEAM && !(p->ramp_periods > 0))
-    return fail(FV_BAD_ARG, "focused beam needs ramp_periods > 0");
+  if ((p->app == FV_APP_FOCUSED_BEAM || p->app == FV_APP_PHASED_ARRAY) && !(p->ramp_periods > 0))
+    return fail(FV_BAD_ARG, "focused beam and phased array need ramp_periods > 0");
+  if (p->app == FV_APP_PHASED_ARRAY) {
+    if (p->array_elems < 1 || p->array_elems > 4096) return fail(FV_BAD_ARG, "array_elems must be 1..4096");
+    const double w = p->aperture / p->array_elems;
+    if (!(w >= 1) || w != std::floor(w)) return fail(FV_BAD_ARG, "aperture must be a multiple of array_elems cells");
+  }
   return FV_OK;
 }
 
@@ -166,6 +175,11 @@ DevParams make_dev_params(const fv_params &p) {
   d.center = float(p.center);
   d.halfap = float(p.aperture * 0.5);
   d.ramp = p.ramp_periods > 0 ? float(p.frec / p.ramp_periods) : 0.0f;
+  if (p.app == FV_APP_PHASED_ARRAY) {
+    d.nelem = p.array_elems;
+    d.arr_elem = int(p.aperture / p.array_elems);
+    d.arr_j0 = int(std::lround(p.center - 0.5 * p.aperture));
+  }
   return d;
 }
 
@@ -401,6 +415,25 @@ fv_status fv_default_params(int32_t app, fv_params *out) {
       p.tide = 0.0;
       break;
     }
+    case FV_APP_PHASED_ARRAY: {
+      // 1024 x 1024, 24 cells per wavelength, 128 elements of 8 cells on
+      // the left edge centred on j = 512, Mach 2e-3 per element reached
+      // over 5 periods
+      p.nx = 1024;
+      p.ny = 1024;
+      p.xmax = 1023.0 / 24.0;
+      p.ymax = 1023.0 / 24.0;
+      p.beta = 3.5;
+      p.diffdelta = 5e-5;
+      p.ampl = 2e-3;
+      p.frec = 1.0;
+      p.array_elems = 128;
+      p.aperture = 1024.0;
+      p.center = 512.0;
+      p.ramp_periods = 5.0;
+      p.tide = 0.0;
+      break;
+    }
     default:
       return fail(FV_BAD_ARG, "unknown app %d", app);
   }
@@ -427,6 +460,18 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   if (!h) return fail(FV_CUDA_ERROR, "out of host memory");
   h->params = *p;
   h->dp = make_dev_params(*p);
+  if (p->app == FV_APP_PHASED_ARRAY) {
+    // every element starts at amplitude AMPL and phase 0
+    std::vector<float> w(2 * size_t(p->array_elems), 0.0f);
+    for (int k = 0; k < p->array_elems; ++k) w[k] = float(p->ampl);
+    cudaError_t ew = cudaMalloc(&h->weights, w.size() * sizeof(float));
+    if (ew == cudaSuccess) ew = cudaMemcpy(h->weights, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (ew != cudaSuccess) {
+      fv_destroy(h);
+      return fail(FV_CUDA_ERROR, "phased-array weights: %s", cudaGetErrorString(ew));
+    }
+    h->dp.weights = h->weights;
+  }
   h->device = dev;
   h->exact = p->exact != 0;
   h->ncell = size_t(p->nx) * size_t(p->ny);
@@ -498,6 +543,9 @@ fv_status fv_destroy(fv_handle *h) {
   if (h->ctrl_host) cudaFreeHost(h->ctrl_host);
   if (h->partials) cudaFree(h->partials);
   if (h->fix) cudaFree(h->fix);
+  if (h->weights) cudaFree(h->weights);
+  if (h->snap_mem) cudaFree(h->snap_mem);
+  if (h->snap_ctrl) cudaFree(h->snap_ctrl);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return FV_OK;
@@ -547,6 +595,46 @@ fv_status fv_set_scalars(fv_handle *h, double dt, double T, int32_t n) {
   if (!h) return fail(FV_BAD_ARG, "handle is NULL");
   ctrl_scalars_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, float(dt), float(T), n);
   FV_CUDA(cudaGetLastError());
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+// The reference keeps a copy of the pre-step state (texCpy, common/
+// main.cu:72-91) and copies it back after a rejected step (restore,
+// :93-107). The step kernel never overwrites its input, so retries need no
+// copy here; fv_snapshot/fv_restore offer the same save-and-return to
+// callers, with the time-stepping scalars.
+fv_status fv_set_array_weights(fv_handle *h, const float *amp, const float *phase, int32_t nelem) {
+  if (!h || !amp || !phase) return fail(FV_BAD_ARG, "NULL argument");
+  if (!h->weights) return fail(FV_BAD_ARG, "not a phased-array simulation");
+  if (nelem != h->dp.nelem) return fail(FV_BAD_ARG, "nelem %d, the array has %d elements", nelem, h->dp.nelem);
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  FV_CUDA(cudaMemcpy(h->weights, amp, size_t(nelem) * sizeof(float), cudaMemcpyHostToDevice));
+  FV_CUDA(cudaMemcpy(h->weights + nelem, phase, size_t(nelem) * sizeof(float), cudaMemcpyHostToDevice));
+  return FV_OK;
+}
+
+fv_status fv_snapshot(fv_handle *h) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (!h->snap_mem) FV_CUDA(cudaMalloc(&h->snap_mem, 3 * h->field_stride * sizeof(float)));
+  if (!h->snap_ctrl) FV_CUDA(cudaMalloc(&h->snap_ctrl, sizeof(Ctrl)));
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  const int cur = h->ctrl_host->cur;
+  FV_CUDA(cudaMemcpyAsync(h->snap_mem, field_ptr(h, cur, 0), 3 * h->field_stride * sizeof(float),
+                          cudaMemcpyDeviceToDevice, h->stream));
+  FV_CUDA(cudaMemcpyAsync(h->snap_ctrl, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToDevice, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  h->snap_cur = cur;
+  return FV_OK;
+}
+
+fv_status fv_restore(fv_handle *h) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (h->snap_cur < 0) return fail(FV_BAD_ARG, "no snapshot taken");
+  FV_CUDA(cudaMemcpyAsync(field_ptr(h, h->snap_cur, 0), h->snap_mem, 3 * h->field_stride * sizeof(float),
+                          cudaMemcpyDeviceToDevice, h->stream));
+  FV_CUDA(cudaMemcpyAsync(h->ctrl, h->snap_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToDevice, h->stream));
   FV_CUDA(cudaStreamSynchronize(h->stream));
   return FV_OK;
 }

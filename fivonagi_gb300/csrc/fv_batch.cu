@@ -139,6 +139,8 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
   *out = nullptr;
   bool exact = params[0].exact != 0;
   for (int k = 0; k < n; ++k) {
+    if (params[k].app == FV_APP_PHASED_ARRAY)
+      return bfail(FV_BAD_ARG, "the phased array is not supported in batches");
     fv_status s = validate_params(&params[k]);
     if (s != FV_OK) return s;
     if ((params[k].exact != 0) != exact) return bfail(FV_BAD_ARG, "all simulations of a batch share `exact`");

@@ -31,6 +31,10 @@ struct DevParams {
   float isprhoa, ispc, mdt;
   float cos_th, sin_th;    // cos/sin(ISPTHETA), evaluated once on the host
   float center, halfap, ramp;
+  // phased array: elements of arr_elem rows from row arr_j0; weights holds
+  // the amplitudes [0, nelem) then the phases [nelem, 2 nelem) (device)
+  int32_t nelem, arr_j0, arr_elem, pad1;
+  const float *weights;
 };
 
 // Device-resident time-stepping state of one simulation. The reference

@@ -95,7 +95,8 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
                                      int32_t mdy, void *cuda_stream, fv_step_result *res) {
   if (!p || !in_u1 || !in_u2 || !in_u3 || !out_u1 || !out_u2 || !out_u3 || !res)
     return nafail(FV_BAD_ARG, "NULL argument");
-  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM) return nafail(FV_BAD_ARG, "unknown app");
+  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM)
+    return nafail(FV_BAD_ARG, "unknown app (the phased array needs fv_create's weights)");
   if (p->nx < 8 || p->ny < 8) return nafail(FV_BAD_ARG, "grid below 8x8");
   if ((long long)p->nx + (long long)p->ny > FV_NOALLOC_MAX_PERIMETER)
     return nafail(FV_BAD_ARG, "nx + ny above FV_NOALLOC_MAX_PERIMETER (the ghost frame's room in the scratch array)");

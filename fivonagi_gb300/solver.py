@@ -84,6 +84,22 @@ class Simulation:
         check(self.lib.fv_get_stats(self.h, C.byref(st)), "fv_get_stats")
         return st.as_dict()
 
+    def set_array_weights(self, amp, phase) -> None:
+        """Phased-array element amplitudes and phases (FP32)."""
+        a = np.ascontiguousarray(amp, np.float32)
+        ph = np.ascontiguousarray(phase, np.float32)
+        fp = C.POINTER(C.c_float)
+        check(self.lib.fv_set_array_weights(self.h, a.ctypes.data_as(fp), ph.ctypes.data_as(fp), int(a.size)),
+              "fv_set_array_weights")
+
+    def snapshot(self) -> None:
+        """Save the state and time-stepping scalars (one slot)."""
+        check(self.lib.fv_snapshot(self.h), "fv_snapshot")
+
+    def restore(self) -> None:
+        """Return to the last snapshot."""
+        check(self.lib.fv_restore(self.h), "fv_restore")
+
     def set_stream(self, stream_ptr: int | None) -> None:
         check(self.lib.fv_set_stream(self.h, stream_ptr), "fv_set_stream")
 

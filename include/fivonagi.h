@@ -54,7 +54,10 @@ typedef enum fv_app {
   FV_APP_HIFU_BEAM = 0,       /* apps/hifu-beam: focused pulsed source, reflecting axis */
   FV_APP_TAYLOR_ANGLE_XY = 1, /* apps/taylor-angle-xy: analytic tanh (Taylor shock) ghosts */
   FV_APP_PLANE_WAVE = 2,      /* oblique sinusoidal plane wave, no-flux y walls */
-  FV_APP_FOCUSED_BEAM = 3     /* focused continuous-wave source, open boundaries */
+  FV_APP_FOCUSED_BEAM = 3,    /* focused continuous-wave source, open boundaries */
+  FV_APP_PHASED_ARRAY = 4     /* array of continuous-wave elements on the left edge, each
+                                 with its own amplitude and phase (fv_set_array_weights),
+                                 open boundaries; the adjoint's design variables */
 } fv_app;
 
 /* Run-time parameter block. Names follow the reference's parameters.h
@@ -71,7 +74,7 @@ typedef struct fv_params {
   int32_t exact;          /* 1: no FMA contraction (bit-identical to the oracle);
                              0: contracted FMAs (within the FP32 tolerance) */
   int32_t max_retries;    /* consecutive rejected attempts before FV_DT_TOO_LARGE */
-  int32_t reserved0;
+  int32_t array_elems;    /* phased array: number of elements (aperture / array_elems cells each) */
   double xmax, ymax;      /* XMAX, YMAX: dx = XMAX/(NX-1), dy = YMAX/(NY-1) (common/main.cu:790-791) */
   double beta;            /* BETA: nonlinearity coefficient */
   double diffdelta;       /* DIFFDELTA: dimensionless dissipation */
@@ -88,9 +91,9 @@ typedef struct fv_params {
   double isp_f;           /* hifu ISPF, focused-beam focal distance: in grid points */
   double isp_rhoa;        /* taylor ISPRHOA */
   double isp_c;           /* taylor ISPC */
-  double aperture;        /* focused beam: aperture width, cells */
-  double center;          /* focused beam: aperture centre, j index */
-  double ramp_periods;    /* focused beam: linear amplitude ramp length, periods */
+  double aperture;        /* focused beam, phased array: aperture width, cells */
+  double center;          /* focused beam, phased array: aperture centre, j index */
+  double ramp_periods;    /* focused beam, phased array: linear amplitude ramp, periods */
 } fv_params;
 
 typedef struct fv_run_stats {
@@ -148,6 +151,53 @@ fv_status fv_get_state(fv_handle *h, float *u1, float *u2, float *u3,
 /* Set or read the scalar time-stepping state (dt, T, n). */
 fv_status fv_set_scalars(fv_handle *h, double dt, double T, int32_t n);
 fv_status fv_get_stats(fv_handle *h, fv_run_stats *out);
+
+/* Phased array (FV_APP_PHASED_ARRAY): element k drives the left ghost
+ * cells of rows [j0 + k*w, j0 + (k+1)*w), w = aperture / array_elems and
+ * j0 = center - aperture/2, with u1 = amp[k] * ramp(T) * sin(2 pi FREC T +
+ * phase[k]), u2 = u1 (u1 + 1), u3 = 0 -- the focused beam's packet at normal
+ * incidence. nelem must equal params.array_elems; host pointers. fv_create
+ * starts every element at amplitude AMPL and phase 0. */
+fv_status fv_set_array_weights(fv_handle *h, const float *amp, const float *phase, int32_t nelem);
+
+/* ---------------------------------------------------------------- adjoint
+ * Discrete adjoint of the step for the phased array's element weights. The
+ * reference has none. The loss is the mean of u1^2 over a window of cells
+ * and over the states after accepted steps step_first..step_last of an
+ * nsteps-step run from rest (T0 = -TIDE); the dt schedule of the forward
+ * run is held fixed in the derivative. fv_adjoint_forward runs the forward
+ * (adaptive dt, recorded), storing a checkpoint every checkpoint_every
+ * steps (0: ceil(sqrt(nsteps))); fv_adjoint_backward returns d loss / d
+ * amplitude and d loss / d phase per element. fv_adjoint_replay runs the
+ * forward again with other weights on the recorded schedule (for finite
+ * differences); a backward pass needs a fv_adjoint_forward after it. Only
+ * FV_APP_PHASED_ARRAY without the moving window. */
+typedef struct fv_adjoint fv_adjoint;
+typedef struct fv_loss_window {
+  int32_t i0, j0;         /* first cell (i, j) of the window */
+  int32_t ni, nj;         /* window size, cells */
+  int64_t step_first;     /* first accepted step (1-based) whose state enters the loss */
+  int64_t step_last;      /* last one */
+} fv_loss_window;
+fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t nsteps,
+                            int32_t checkpoint_every, fv_adjoint **out);
+fv_status fv_adjoint_destroy(fv_adjoint *a);
+fv_status fv_adjoint_set_stream(fv_adjoint *a, void *cuda_stream);
+fv_status fv_adjoint_forward(fv_adjoint *a, const float *amp, const float *phase, double *loss);
+fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phase);
+fv_status fv_adjoint_replay(fv_adjoint *a, const float *amp, const float *phase, double *loss);
+/* The recorded schedule: dt and T (before the step) of each of the nsteps steps. */
+fv_status fv_adjoint_schedule(fv_adjoint *a, double *dt, double *T);
+/* The state after the last forward or replay (host buffers of NX*NY floats). */
+fv_status fv_adjoint_get_state(fv_adjoint *a, float *u1, float *u2, float *u3);
+
+/* Save the current state and time-stepping scalars (dt, T, n, window
+ * offsets, retry state) in the handle's one snapshot slot, overwriting it;
+ * fv_restore brings them back. Replaces the reference's texCpy/restore
+ * pair (common/main.cu:72-107), which keeps the pre-step state to retry a
+ * rejected step. fv_restore without a snapshot returns FV_BAD_ARG. */
+fv_status fv_snapshot(fv_handle *h);
+fv_status fv_restore(fv_handle *h);
 
 /* Use a caller-provided cudaStream_t (passed as void*); NULL = the
  * library's own stream. */

@@ -41,6 +41,14 @@ Sim<R>::Sim(const fv_params &pp, bool fvm_math) : p(pp), fvm_mode(fvm_math) {
   ac.aperture = R(p.aperture * 0.5);  // half aperture, cells
   ac.center = R(p.center);
   ac.ramp = R(p.frec / p.ramp_periods);
+  if (p.app == FV_APP_PHASED_ARRAY) {
+    // element k drives rows [arr_j0 + k*arr_elem, arr_j0 + (k+1)*arr_elem)
+    ac.nelem = p.array_elems;
+    ac.arr_elem = int(p.aperture / p.array_elems);
+    ac.arr_j0 = int(std::lround(p.center - 0.5 * p.aperture));
+    ac.amp.assign(size_t(ac.nelem), R(p.ampl));
+    ac.phase.assign(size_t(ac.nelem), R(0));
+  }
   for (int f = 0; f < 3; ++f) {
     u[f].assign(size(), R(0));
     s0[f].assign(size(), R(0));
@@ -173,6 +181,20 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
             } else {
               take(2, j);
             }
+          } else if (app == FV_APP_PHASED_ARRAY) {
+            // phased array: the focused beam's packet at normal incidence,
+            // with each element's own amplitude and phase
+            const int jr = j - ac.arr_j0;
+            if (jr >= 0 && jr < ac.nelem * ac.arr_elem && mdx == 0) {
+              const int e = jr / ac.arr_elem;
+              R ramp = getmin(getmax(T * ac.ramp, zero), one);
+              R pack = ac.amp[e] * ramp * Fn<R>::sin(ac.ispw * T + ac.phase[e], fvm_mode);
+              v1 = pack;
+              v2 = pack * (pack + one);
+              v3 = zero;
+            } else {
+              take(2, j);
+            }
           } else if (app == FV_APP_FOCUSED_BEAM) {
             R jp = R(j) - ac.center;
             if (std::fabs(jp) < ac.aperture && mdx == 0) {
@@ -194,7 +216,7 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
             take(2, j);  // plane wave: zero-order extrapolation
           }
         } else {  // j <= 1
-          if (app == FV_APP_FOCUSED_BEAM) {
+          if (app == FV_APP_FOCUSED_BEAM || app == FV_APP_PHASED_ARRAY) {
             take(i, 2);  // open lateral side, common/boundary.h:41-53
           } else {
             take(i, 4 - j);  // reflecting, hifu :110-122
@@ -509,6 +531,23 @@ int fvo_set_scalars(void *hv, double dt, double T, int n) {
     s.n = n;
   });
   return FV_OK;
+}
+
+// Phased-array element weights (amplitudes, phases), given in double.
+int fvo_set_weights(void *hv, const double *amp, const double *phase, int nelem) {
+  Handle *h = static_cast<Handle *>(hv);
+  int rc = 0;
+  FVO_DISPATCH(h, {
+    if (nelem != s.ac.nelem) {
+      rc = 1;
+    } else {
+      for (int k = 0; k < nelem; ++k) {
+        s.ac.amp[k] = decltype(s.dt)(amp[k]);
+        s.ac.phase[k] = decltype(s.dt)(phase[k]);
+      }
+    }
+  });
+  return rc;
 }
 
 int fvo_get_stats(void *hv, fv_run_stats *st) {

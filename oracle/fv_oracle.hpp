@@ -192,6 +192,8 @@ template <class R> struct AppConsts {
   R isprhoa, ispc, isptheta, mdt;          // taylor
   R angle;                                 // plane wave
   R aperture, center, ramp;                // focused beam
+  int nelem = 0, arr_j0 = 0, arr_elem = 1;  // phased array
+  std::vector<R> amp, phase;
 };
 
 template <class R> class Sim {

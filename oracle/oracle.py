@@ -62,6 +62,8 @@ def _load_oracle() -> C.CDLL:
         lib.fvo_last_cfl.restype = C.c_double
         lib.fvo_last_cfl.argtypes = [P]
         lib.fvo_fvm_eval.argtypes = [C.c_int, P, P, C.c_int64]
+        lib.fvo_set_weights.restype = C.c_int
+        lib.fvo_set_weights.argtypes = [P, P, P, C.c_int]
         _oracle = lib
     return _oracle
 
@@ -142,6 +144,13 @@ class OracleSim:
 
     def set_scalars(self, dt, T, n=0):
         self.lib.fvo_set_scalars(self.h, float(dt), float(T), int(n))
+
+    def set_weights(self, amp, phase):
+        """Phased-array element amplitudes and phases."""
+        a = np.ascontiguousarray(amp, np.float64)
+        ph = np.ascontiguousarray(phase, np.float64)
+        if self.lib.fvo_set_weights(self.h, _ptr(a), _ptr(ph), int(a.size)) != 0:
+            raise ValueError("weights do not match the phased array")
 
     def stats(self) -> dict:
         st = FvRunStats()

@@ -30,12 +30,27 @@ def small_params(app: int, nx: int, ny: int, exact: int = 1) -> FvParams:
         p.xmax, p.ymax = (nx - 1) / 16, (ny - 1) / 16
         p.beta, p.diffdelta = 3.5, 1e-4
         p.ampl, p.frec, p.angle, p.tide = 1e-2, 1.0, np.pi / 6, 0.0
-    else:  # focused beam
+    elif app == 3:  # focused beam
         p.xmax, p.ymax = (nx - 1) / 16, (ny - 1) / 16
         p.beta, p.diffdelta = 3.5, 5e-5
         p.ampl, p.frec, p.isp_f = 5e-2, 1.0, 60.0
         p.aperture, p.center, p.ramp_periods, p.tide = ny / 2, ny / 2, 1.0, 0.0
+    else:  # phased array: 8 elements over about half the left edge
+        p.xmax, p.ymax = (nx - 1) / 16, (ny - 1) / 16
+        p.beta, p.diffdelta = 3.5, 5e-5
+        p.ampl, p.frec = 5e-2, 1.0
+        p.array_elems = 8
+        p.aperture = 8 * max(1, (ny // 2) // 8)
+        p.center, p.ramp_periods, p.tide = ny / 2, 1.0, 0.0
     return p
+
+
+def array_weights(nelem: int, seed: int, ampl: float):
+    """Element amplitudes ~ U[0.5, 1.5] * ampl and phases ~ U[0, 2 pi), FP32."""
+    rng = np.random.default_rng(seed)
+    amp = (rng.uniform(0.5, 1.5, nelem) * ampl).astype(np.float32)
+    ph = rng.uniform(0.0, 2 * np.pi, nelem).astype(np.float32)
+    return amp, ph
 
 
 def rel_l2(a, b) -> float:

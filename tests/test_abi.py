@@ -86,6 +86,8 @@ def test_workload_defaults():
     fb = _abi.default_params("focused-beam")
     assert (fb.nx, fb.ny) == (4096, 2048) and fb.xmax == 4095 / 24
     assert fb.aperture == 1024 and fb.center == 1024 and fb.isp_f == 3000 and fb.ramp_periods == 5
+    pa = _abi.default_params("phased-array")
+    assert (pa.nx, pa.ny, pa.array_elems) == (1024, 1024, 128) and pa.aperture / pa.array_elems == 8
 
 
 def test_bad_arguments_are_rejected_before_any_device_work():
@@ -93,7 +95,9 @@ def test_bad_arguments_are_rejected_before_any_device_work():
     h = C.c_void_p()
     p = _abi.default_params("plane-wave")
     for bad in (p.replace(nx=4), p.replace(app=9), p.replace(xmax=-1.0), p.replace(dtini=0.0),
-                _abi.default_params("focused-beam").replace(ramp_periods=0.0)):
+                _abi.default_params("focused-beam").replace(ramp_periods=0.0),
+                _abi.default_params("phased-array").replace(array_elems=0),
+                _abi.default_params("phased-array").replace(array_elems=100)):
         assert lib.fv_create(C.byref(bad), C.byref(h)) == _abi.FV_BAD_ARG
         assert lib.fv_last_error_string()
     assert lib.fv_create(None, C.byref(h)) == _abi.FV_BAD_ARG
@@ -113,3 +117,18 @@ def test_no_device_is_a_status_not_a_crash():
     with pytest.raises(_abi.FvError):
         from fivonagi_gb300 import Simulation
         Simulation(p)
+
+
+def test_restore_without_snapshot_is_bad_arg_without_device():
+    # no device here: fv_create fails first; the argument check on a NULL
+    # handle needs no device
+    lib = _abi.load_library()
+    assert lib.fv_restore(None) == _abi.FV_BAD_ARG
+    assert lib.fv_snapshot(None) == _abi.FV_BAD_ARG
+
+
+def test_adjoint_rejects_null_arguments_without_device():
+    lib = _abi.load_library()
+    assert lib.fv_adjoint_create(None, None, 10, 0, None) == _abi.FV_BAD_ARG
+    assert lib.fv_adjoint_backward(None, None, None) == _abi.FV_BAD_ARG
+    assert lib.fv_adjoint_destroy(None) == _abi.FV_OK

@@ -1,0 +1,108 @@
+"""The discrete adjoint of the phased array's windowed loss.
+
+The forward the adjoint records is the library's ordinary step, so its final
+state equals fv_run's bit for bit. The gradient is checked against central
+differences of the FP64 oracle run on the forward's recorded dt schedule
+(the adjoint holds that schedule fixed).
+"""
+import numpy as np
+import pytest
+
+from fivonagi_gb300 import Simulation
+from fivonagi_gb300.adjoint import Adjoint, array_loss_function, loss_window
+from oracle.oracle import OracleSim
+from tests.helpers import array_weights, same_values, small_params
+
+pytestmark = pytest.mark.gpu
+
+NX, NY, NSTEPS = 64, 48, 120
+WIN = (14, 18, 8, 8, 60, NSTEPS)  # i0, j0, ni, nj, first, last
+
+
+def _params():
+    return small_params(4, NX, NY)
+
+
+def _oracle_loss(p, amp, ph, dts, Ts):
+    """The loss of the FP64 oracle on a fixed dt schedule."""
+    q = p.replace(cflmax=1e30)
+    o = OracleSim(q, np.float64)
+    o.set_weights(np.asarray(amp, np.float64), np.asarray(ph, np.float64))
+    o.init_state()
+    i0, j0, ni, nj, first, last = WIN
+    acc = 0.0
+    for n in range(NSTEPS):
+        o.set_scalars(dts[n], Ts[n], n)
+        st = o.run(1)
+        assert st["rc"] == 0 and st["accepted"] == 1
+        if first <= n + 1 <= last:
+            u1 = o.get_state()[0]
+            acc += float(np.sum(u1[j0:j0 + nj, i0:i0 + ni] ** 2))
+    return acc / ((last - first + 1) * ni * nj)
+
+
+def test_adjoint_forward_is_the_plain_step_and_replay_reproduces_it():
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 11, p.ampl)
+    adj = Adjoint(p, loss_window(*WIN), NSTEPS, checkpoint_every=16)
+    loss = adj.forward(amp, ph)
+    sim = Simulation(p)
+    sim.set_array_weights(amp, ph)
+    sim.init_state()
+    sim.run(NSTEPS)
+    g, r = adj.get_state(), sim.get_state()
+    for f in range(3):
+        assert same_values(g[f], r[f])
+    dts, Ts = adj.schedule()
+    assert np.all(dts > 0) and np.all(np.diff(Ts) > 0)
+    assert adj.replay(amp, ph) == loss
+    assert loss > 0
+    sim.close()
+    adj.close()
+
+
+def test_adjoint_gradient_matches_fp64_central_differences():
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 11, p.ampl)
+    adj = Adjoint(p, loss_window(*WIN), NSTEPS, checkpoint_every=16)
+    loss = adj.forward(amp, ph)
+    ga, gp = adj.backward()
+    dts, Ts = adj.schedule()
+    adj.close()
+    # the FP64 oracle's loss on the same schedule is the FP32 loss to a few ulps
+    l64 = _oracle_loss(p, amp, ph, dts, Ts)
+    assert abs(l64 - loss) <= 1e-4 * loss
+    g64 = []
+    for k in (0, 3, 5, 7):
+        for which in ("amp", "phase"):
+            a = amp.astype(np.float64).copy()
+            f = ph.astype(np.float64).copy()
+            v = a if which == "amp" else f
+            h = 1e-4 * (abs(v[k]) if which == "amp" else 1.0)
+            v[k] += h
+            lp = _oracle_loss(p, a, f, dts, Ts)
+            v[k] -= 2 * h
+            lm = _oracle_loss(p, a, f, dts, Ts)
+            fd = (lp - lm) / (2 * h)
+            got = ga[k] if which == "amp" else gp[k]
+            g64.append((which, k, got, fd))
+    scale = max(abs(fd) for *_, fd in g64)
+    assert scale > 0
+    for which, k, got, fd in g64:
+        assert abs(got - fd) <= 2e-3 * scale, (which, k, got, fd)
+
+
+def test_torch_function_returns_the_adjoint_gradients():
+    torch = pytest.importorskip("torch")
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 4, p.ampl)
+    adj = Adjoint(p, loss_window(*WIN), NSTEPS)
+    fn = array_loss_function()
+    ta = torch.tensor(amp, dtype=torch.float32, requires_grad=True)
+    tp = torch.tensor(ph, dtype=torch.float32, requires_grad=True)
+    loss = fn.apply(ta, tp, adj)
+    (3.0 * loss).backward()
+    ga, gp = adj.backward()
+    np.testing.assert_allclose(ta.grad.numpy(), np.float32(3.0 * ga), rtol=1e-6)
+    np.testing.assert_allclose(tp.grad.numpy(), np.float32(3.0 * gp), rtol=1e-6)
+    adj.close()

@@ -222,3 +222,51 @@ def test_moving_domain_matches_oracle(app, mdt, nsteps):
     for f in range(3):
         assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
     sim.close()
+
+
+@pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (0, 100, 37)])
+def test_snapshot_restore_replays_bit_for_bit(app, nx, ny):
+    """fv_snapshot / fv_restore (the reference's texCpy/restore pair): the
+    steps after a restore reproduce the steps after the snapshot exactly,
+    state and time-stepping scalars alike."""
+    p = small_params(app, nx, ny)
+    sim = Simulation(p)
+    sim.init_state()
+    sim.run(5)
+    sim.snapshot()
+    sim.run(7)
+    first, st1 = sim.get_state(), sim.stats()
+    sim.restore()
+    st0 = sim.stats()
+    assert st0["n"] == 5
+    sim.run(7)
+    second, st2 = sim.get_state(), sim.stats()
+    for f in range(3):
+        assert same_values(first[f], second[f])
+    for k in ("dt", "T", "n", "mdx", "mdy"):
+        assert st1[k] == st2[k], k
+    sim.close()
+
+
+@pytest.mark.parametrize("nx,ny", [(96, 64), (130, 77)])
+def test_phased_array_matches_oracle(nx, ny):
+    """The phased-array app with random element weights, bit for bit."""
+    from tests.helpers import array_weights
+
+    p = small_params(4, nx, ny)
+    amp, ph = array_weights(p.array_elems, 5, p.ampl)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.set_weights(amp, ph)
+    orc.init_state()
+    sim = Simulation(p)
+    sim.set_array_weights(amp, ph)
+    sim.init_state()
+    so = orc.run(60)
+    st = sim.run(60)
+    assert st["accepted"] == so["accepted"] == 60
+    assert np.float32(st["T"]) == np.float32(so["T"]) and np.float32(st["dt"]) == np.float32(so["dt"])
+    g, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
+    assert np.abs(g[0]).max() > 1e-3  # the source reached the grid
+    sim.close()
