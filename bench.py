@@ -351,8 +351,8 @@ def run_gpu(args):
         },
         "roofline": roofline,
         "e2e": e2e,
-        # per attempt: ghost-frame pre-pass, step kernel, fix-up kernel
-        "gpu_launches": 3 * (accepted + int(st["rejected"])),
+        # per attempt: ghost-frame pre-pass, step, fix-up, finalize
+        "gpu_launches": 4 * (accepted + int(st["rejected"])),
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
@@ -437,8 +437,8 @@ def run_batched(args):
         "sequential_plain_path": {"value": seq_rate, "unit": "Gcell-updates/s", "ms_total": ms_seq},
         "batched_over_sequential": batched_rate / seq_rate,
         "clocks": clocks,
-        # per attempt: ghost-frame pre-pass, batch step kernel, batch fix-up kernel
-        "gpu_launches": 3 * steps,
+        # per attempt: ghost-frame pre-pass, batch step, batch fix-up, batch finalize
+        "gpu_launches": 4 * steps,
     }
     print(json.dumps(line))
     return 0

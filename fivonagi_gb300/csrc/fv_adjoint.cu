@@ -12,14 +12,15 @@
 // (apps/na/fv.h), D the diffusion (apps/na/source.h). The loss is the mean
 // of u1^2 over a window of cells and a range of accepted steps.
 //
-// Forward: the ordinary attempt launches (ghost frame, step, fix-up), with
+// Forward: the ordinary attempt launches (ghost frame, step, fix-up,
+// finalize), with
 // three one-thread kernels around each attempt that record the dt and T of
 // accepted steps, copy a checkpoint every C accepted steps and add the
 // step's window sum to the loss -- all device-side, no host round trip per
 // step. Backward: segment by segment from the last checkpoint, replay the
 // segment's steps from its checkpoint (frozen dt) into a buffer of C
 // states, then walk the segment backwards. A reverse step recomputes the
-// forward stages B, Y, X of its input with the stage kernels and runs
+// forward stages B, Y, X of its input in one stage-kernel pass and runs
 // grid-wide reverse kernels: diffusion, x sweep, y sweep (three kernels
 // each: waves, interface adjoints, per-cell gather), boundary (ghost cells
 // back to the cells they copy, and the source cells to the weights).
@@ -765,10 +766,12 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
       for (int f = 0; f < 3; ++f) in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
       const float dt = a->h_dt[n - 1], T = a->h_T[n - 1];
       adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0);
-      for (int st = 0; st < 3; ++st) {
+      {
+        // boundary-applied state, y-swept and x-swept state in one pass
         StepArgs s = step_args(a, a->dp_replay, in, in);
-        for (int f = 0; f < 3; ++f) s.dbg[f] = a->stage[st][f];
-        const int rc = launch(a, s, st);  // 0: boundary, 1: y sweep, 2: x sweep
+        for (int st = 0; st < 3; ++st)
+          for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = a->stage[st][f];
+        const int rc = launch(a, s, kStageAll);
         if (rc != 0) return afail(FV_CUDA_ERROR, "stage launch: %s", cudaGetErrorString((cudaError_t)rc));
       }
       float *const *lo = a->lam[lc];

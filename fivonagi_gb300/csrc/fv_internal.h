@@ -56,7 +56,7 @@ struct Ctrl {
   int64_t remaining;      // accepted steps still to take; 0 = idle
   int64_t accepted;       // counters since the last fv_run/fv_sync reset
   int64_t rejected;
-  uint32_t blocks_done;   // last-block-done counter of the current attempt
+  uint32_t blocks_done;   // unused (zero)
   uint32_t pad;
 };
 
@@ -82,6 +82,11 @@ __host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny
 //   bitmap of marked chunks (one bit per chunk), then the list of marked
 //   chunk ids (window * chunks_per_window + chunk), one per marked chunk.
 constexpr int kFixRows = 8;
+
+// Stage kernel of the adjoint's recompute: one pass writing the
+// boundary-applied state, the state after the y sweep and after the x
+// sweep (StepArgs::stages), exact (IEEE-equal) division.
+constexpr int kStageAll = 4;
 __host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }
@@ -100,7 +105,8 @@ struct StepArgs {
   Ctrl *ctrl;
   float *partials;        // one CFL maximum per CTA of the step launch, then
                           // one per CTA of the fix-up launch
-  float *dbg[3];          // debug-stage output (stage kernels only)
+  float *dbg[3];          // debug-stage output (stage kernels 0..3 only)
+  float *stages[9];       // kStageAll output: boundary-applied state, y-swept, x-swept
   uint32_t *fix;          // fix-up scratch, zero between attempts (see above)
   int32_t nstrips;        // column strips of width kWarpCols * warps
   int32_t nblocks;        // CTAs of the launch

@@ -301,6 +301,12 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     if (STAGE == FV_STAGE_BOUNDARY || STAGE == FV_STAGE_SWEEP_Y) {
       if (out_lane && cyr >= y0 && cyr < y1) store3(out, i + cyr * nx, STAGE == FV_STAGE_BOUNDARY ? s0_m2 : s1);
     }
+    if (STAGE == kStageAll) {
+      if (out_lane && cyr >= y0 && cyr < y1) {
+        store3(out, i + cyr * nx, s0_m2);
+        store3(out + 3, i + cyr * nx, s1);
+      }
+    }
 
     // ---- X results
     const int cxr = r - 3;
@@ -314,6 +320,9 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     }
     if (STAGE == FV_STAGE_SWEEP_X) {
       if (own_x) store3(out, i + cxr * nx, xo.s2);
+    }
+    if (STAGE == kStageAll) {
+      if (own_x) store3(out + 6, i + cxr * nx, xo.s2);
     }
 
     // ======== D chain: diffusion of row r-5 (apps/na/source.h:22-104)
@@ -426,12 +435,12 @@ __device__ __forceinline__ bool attempt_active(const Ctrl *ctl) {
   return status == 0 && remaining > 0 && T0 < ts;
 }
 
-// Reduce the partial CFL maxima of the step and fix-up launches and
-// decide; runs on the last CTA of the fix-up launch (all its threads).
+// Reduce the partial CFL maxima of the step launch (and of the fix-up
+// launch, when it had chunks to do) and decide; one CTA (all its threads).
 __device__ void finalize(const StepArgs &a, float *red) {
   Ctrl *ctl = a.ctrl;
   float m = 0.0f;
-  const int np = a.nblocks + a.fix_blocks;
+  const int np = a.nblocks + (__ldcg(a.fix) > 0u ? a.fix_blocks : 0);
   for (int b = threadIdx.x; b < np; b += blockDim.x) m = nanmax(m, __ldcg(a.partials + b));
   for (int off = 16; off > 0; off >>= 1) m = nanmax(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -447,7 +456,6 @@ __device__ void finalize(const StepArgs &a, float *red) {
   fx[0] = 0u;
   fx[1] = 0u;
   __threadfence();
-  vc->blocks_done = 0;
 }
 
 // Shift of the moving window this attempt applies if it is accepted:
@@ -482,11 +490,9 @@ __device__ __forceinline__ void stream_window(const DevParams &p, const float *c
 }
 
 // The CTA's CFL maximum into partials[slot], and the negative-eigenvalue
-// flag into the control block. With `count`, returns (to every thread)
-// whether this CTA is the last of `nblocks` to get here, counted on the
-// control block's blocks_done.
-__device__ __forceinline__ bool publish(const StepArgs &a, float cmax, bool neg, int slot,
-                                        int nblocks, bool count, float *red, int *sh) {
+// flag into the control block.
+__device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg, int slot, float *red,
+                                        int *sh) {
   const int warp = threadIdx.x >> 5;
   for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
   if (threadIdx.x == 0) sh[0] = 0;
@@ -499,24 +505,17 @@ __device__ __forceinline__ bool publish(const StepArgs &a, float cmax, bool neg,
     for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
     a.partials[slot] = m;
     if (sh[0]) ((volatile Ctrl *)a.ctrl)->neg_flag = 1;
-    sh[1] = 0;
-    if (count) {
-      __threadfence();
-      const unsigned prev = atomicAdd(&a.ctrl->blocks_done, 1u);
-      sh[1] = (prev == (unsigned)(nblocks - 1)) ? 1 : 0;
-    }
   }
-  __syncthreads();
-  return sh[1] != 0;
 }
 
 // The step: STAGE < 0 is the full attempt with FMA division, followed by
-// the fix-up launch; STAGE 0..3 write that stage's grid to the debug
-// buffers with IEEE division.
+// the fix-up and finalize launches; STAGE 0..3 write that stage's grid to
+// the debug buffers with IEEE division; kStageAll writes the first three
+// stages' grids at once (the adjoint's recompute).
 template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   __shared__ float red[kWarps];
-  __shared__ int sh[2];
+  __shared__ int sh[1];
   const Ctrl *ctl = a.ctrl;
   // Uniform early exit: the control block only changes between launches.
   if (STAGE < 0 && !attempt_active(ctl)) return;
@@ -527,8 +526,12 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   int shx = 0, shy = 0;
   if (STAGE < 0) window_shift(a.p, T, dt, mdx, mdy, shx, shy);
   const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
-  float *out[3];
-  for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
+  float *out[STAGE == kStageAll ? 9 : 3];
+  if constexpr (STAGE == kStageAll) {
+    for (int k = 0; k < 9; ++k) out[k] = a.stages[k];
+  } else {
+    for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
+  }
   const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
   using DP = typename std::conditional<(STAGE < 0), DivFma, DivIEEE>::type;
 
@@ -549,6 +552,15 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
       if constexpr (STAGE < 0) {
         StepMarker mk{a, -1};
         stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+      } else if constexpr (STAGE == kStageAll) {
+        // exact division without branches; a warp whose operands leave
+        // DivExact's range redoes its segment with IEEE division
+        FlagMarker fm;
+        stream_window<STAGE, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, fm);
+        if (__any_sync(0xffffffffu, fm.flagged)) {
+          NoMarker mk;
+          stream_window<STAGE, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+        }
       } else {
         NoMarker mk;
         stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
@@ -557,11 +569,11 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     pos += y1 - y0;
   }
   if (STAGE >= 0) return;
-  publish(a, cmax, neg, blockIdx.x, a.nblocks, false, red, sh);
+  publish(a, cmax, neg, blockIdx.x, red, sh);
 }
 
 // Recomputes the chunks the step launch marked, with exact division
-// (DivExact), then decides the attempt on its last CTA. Each chunk is split
+// (DivExact), before finalize_kernel decides the attempt. Each chunk is split
 // into items of kFixItemRows rows; warps take items from a shared cursor.
 // The rows of an item are a serial loop (plus the pipeline's 8 rows of
 // warm-up and drain) that runs with few other warps on its SM, so its
@@ -573,7 +585,7 @@ static_assert(kFixRows % kFixItemRows == 0, "fix-up items must tile a chunk");
 
 __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
   __shared__ float red[kWarps];
-  __shared__ int sh[2];
+  __shared__ int sh[1];
   const Ctrl *ctl = a.ctrl;
   if (!attempt_active(ctl)) return;
   const float dt = __ldcg(&ctl->dt);
@@ -592,11 +604,12 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
   const uint32_t *list = a.fix + 4 + bitmap_words;
   constexpr unsigned kItems = kFixRows / kFixItemRows;  // items per chunk
   const unsigned n = __ldcg(a.fix) * kItems;
+  if (n == 0u) return;  // nothing marked: the finalize launch reads the step's partials only
   float cmax = 0.0f;
   bool neg = false;
   for (;;) {
     unsigned k = n;
-    if (lane == 0 && n > 0u) k = atomicAdd(a.fix + 1, 1u);
+    if (lane == 0) k = atomicAdd(a.fix + 1, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
     if (k >= n) break;
     const unsigned id = __ldcg(list + k / kItems);
@@ -619,10 +632,15 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
     cmax = nanmax(cmax, cm);
     neg = neg || ng;
   }
-  if (publish(a, cmax, neg, a.nblocks + blockIdx.x, a.fix_blocks, true, red, sh)) {
-    __threadfence();
-    finalize(a, red);
-  }
+  publish(a, cmax, neg, a.nblocks + blockIdx.x, red, sh);
+}
+
+// Decides the attempt after the step and fix-up launches: one CTA, so no
+// CTA of the wide launches has to count who finishes last.
+__global__ void __launch_bounds__(kThreads) finalize_kernel(StepArgs a) {
+  __shared__ float red[kWarps];
+  if (!attempt_active(a.ctrl)) return;
+  finalize(a, red);
 }
 
 // The app's boundary hook (boundary(), apps/*/boundary.h) evaluated for
@@ -785,19 +803,18 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
 
 // The batch's fix-up launch: recomputes the marked chunks of every
 // simulation in items of kFixItemRows rows with exact division (as
-// fixup_kernel), folds their CFL and eigenvalue checks into the
-// simulation's atomics, and on its last CTA decides every active
-// simulation's attempt and clears the per-simulation accumulators.
+// fixup_kernel) and folds their CFL and eigenvalue checks into the
+// simulation's atomics; batch_finalize_kernel then decides.
 __global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
-  __shared__ int is_last;
   const int lane = threadIdx.x & 31;
   constexpr unsigned kItems = kFixRows / kFixItemRows;
   const long long words = (b.fix_chunks + 31) / 32;
   const uint32_t *list = b.fix + 4 + words;
   const unsigned n = __ldcg(b.fix) * kItems;
+  if (n == 0u) return;
   for (;;) {
     unsigned k = n;
-    if (lane == 0 && n > 0u) k = atomicAdd(b.fix + 1, 1u);
+    if (lane == 0) k = atomicAdd(b.fix + 1, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
     if (k >= n) break;
     const unsigned e = k / kItems;
@@ -840,15 +857,11 @@ __global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
       if (wneg) atomicExch(b.neg + inst, 1);
     }
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(b.fix + 2, 1u);
-    is_last = (prev == (unsigned)(b.fix_blocks - 1)) ? 1 : 0;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
+}
+
+// Decides every active simulation's attempt after the batch step and fix-up
+// launches, and clears the per-simulation accumulators; one CTA.
+__global__ void __launch_bounds__(256) batch_finalize_kernel(BatchArgs b) {
   for (int k = threadIdx.x; k < b.n; k += blockDim.x) {
     const BatchInst &I = b.inst[k];
     if (!attempt_active(I.ctrl)) continue;
@@ -861,7 +874,6 @@ __global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
     volatile uint32_t *fx = b.fix;
     fx[0] = 0u;
     fx[1] = 0u;
-    fx[2] = 0u;
     __threadfence();
   }
 }
@@ -872,6 +884,7 @@ static int launch_batch_impl(const BatchArgs &b, void *stream) {
   batch_frame_kernel<<<fgrid, 256, 0, st>>>(b);
   batch_step_kernel<<<b.nblocks, kThreads, 0, st>>>(b);
   batch_fixup_kernel<<<b.fix_blocks, kThreads, 0, st>>>(b);
+  batch_finalize_kernel<<<1, 256, 0, st>>>(b);
   return (int)cudaGetLastError();
 }
 
@@ -893,11 +906,13 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
     case -1:
       step_kernel<-1><<<grid, block, 0, st>>>(a);
       fixup_kernel<<<a.fix_blocks, block, 0, st>>>(a);
+      finalize_kernel<<<1, block, 0, st>>>(a);
       break;
     case 0: step_kernel<0><<<grid, block, 0, st>>>(a); break;
     case 1: step_kernel<1><<<grid, block, 0, st>>>(a); break;
     case 2: step_kernel<2><<<grid, block, 0, st>>>(a); break;
     case 3: step_kernel<3><<<grid, block, 0, st>>>(a); break;
+    case kStageAll: step_kernel<kStageAll><<<grid, block, 0, st>>>(a); break;
     default: return (int)cudaErrorInvalidValue;
   }
   return (int)cudaGetLastError();
