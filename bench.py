@@ -444,6 +444,162 @@ def run_batched(args):
     return 0
 
 
+def _adjoint_case(p, target, nsteps, seed):
+    """Weights and loss window of one design: amplitudes ~ U[0.5, 1.5]
+    AMPL and phases ~ U[0, 2 pi) (seeded), a 32x32 window centred on
+    `target`, the last 500 steps."""
+    import numpy as np
+
+    from fivonagi_gb300.adjoint import loss_window
+
+    rng = np.random.default_rng(seed)
+    amp = (rng.uniform(0.5, 1.5, p.array_elems) * p.ampl).astype(np.float32)
+    ph = rng.uniform(0.0, 2 * np.pi, p.array_elems).astype(np.float32)
+    i, j = target
+    win = loss_window(i - 16, j - 16, 32, 32, max(1, nsteps - 499), nsteps)
+    return amp, ph, win
+
+
+def _device_mem_used():
+    import torch
+
+    free, total = torch.cuda.mem_get_info()
+    return total - free
+
+
+def _time_design(p, amp, ph, win, nsteps, fd_params=0):
+    """Plain forward, recorded forward and backward of one design (wall
+    clock around synchronous calls), and optionally a central-difference
+    check of a few amplitude gradients on the recorded dt schedule."""
+    import numpy as np
+    import torch
+
+    from fivonagi_gb300 import Simulation
+    from fivonagi_gb300.adjoint import Adjoint
+
+    sim = Simulation(p)
+    sim.set_array_weights(amp, ph)
+    sim.init_state()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.run(nsteps)
+    t_plain = time.perf_counter() - t0
+    sim.close()
+    mem0 = _device_mem_used()
+    adj = Adjoint(p, win, nsteps)
+    t0 = time.perf_counter()
+    loss = adj.forward(amp, ph)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ga, gp = adj.backward()
+    t_bwd = time.perf_counter() - t0
+    mem = _device_mem_used() - mem0
+    checks = []
+    order = np.argsort(-np.abs(ga))
+    for k in order[:fd_params]:
+        h = 1e-2 * abs(float(amp[k]))
+        a = amp.astype(np.float64).copy()
+        a[k] += h
+        lp = adj.replay(a.astype(np.float32), ph)
+        a[k] -= 2 * h
+        lm = adj.replay(a.astype(np.float32), ph)
+        hk = (np.float32(amp[k] + h) - np.float32(amp[k] - h)) / 2.0
+        fd = (lp - lm) / (2.0 * float(hk))
+        checks.append({"param": f"amp[{int(k)}]", "adjoint": float(ga[k]), "central_difference": fd,
+                       "rel_diff": abs(float(ga[k]) - fd) / max(abs(fd), 1e-300)})
+    adj.close()
+    return dict(loss=loss, t_plain=t_plain, t_fwd=t_fwd, t_bwd=t_bwd, mem=mem, ga=ga, gp=gp, checks=checks)
+
+
+def run_adjoint(args):
+    """Config 4: the phased array (1024x1024, 128 elements of 8 cells),
+    gradient of the mean u1^2 over a 32x32 window at (700, 512) and steps
+    3501-4000 with respect to the 256 element weights, dt schedule frozen."""
+    from fivonagi_gb300 import _abi
+
+    p = _abi.default_params("phased-array")
+    nsteps = 4000
+    _time_design(p, *_adjoint_case(p, (700, 512), 200, args.seed), 200)  # warm-up: first launches
+    amp, ph, win = _adjoint_case(p, (700, 512), nsteps, args.seed)
+    r = _time_design(p, amp, ph, win, nsteps, fd_params=2)
+    cells = p.nx * p.ny
+    bytes_bwd = 96.0 * cells * nsteps  # algorithmic bytes per cell-step of the adjoint
+    peak, kind = measured_peak()
+    achieved = bytes_bwd / r["t_bwd"] / 1e9
+    line = {
+        "metric": "adjoint/forward time ratio",
+        "value": r["t_bwd"] / r["t_plain"],
+        "unit": "ratio",
+        "n_gpus": 1,
+        "steps": nsteps,
+        "warmup": 200,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "phased array 1024x1024, 128 elements x (amplitude, phase), loss window 32x32 "
+                               "at (700, 512) over steps 3501-4000, checkpoint every ceil(sqrt(N)) steps",
+                   "seed": args.seed},
+        "forward_plain_s": r["t_plain"],
+        "forward_recorded_s": r["t_fwd"],
+        "backward_s": r["t_bwd"],
+        "gradients_per_s": 1.0 / (r["t_fwd"] + r["t_bwd"]),
+        "loss": r["loss"],
+        "adjoint_memory_gb": r["mem"] / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
+                     "traffic": None, "kernel": "backward pass (96 B per cell-step)"},
+        "gradient_check": r["checks"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_designs(args):
+    """Config 5: designs of the phased array on 2048x1024 (6000 steps), each
+    with its own random weights and a focal target from an 8x8 grid in the
+    right half (a seeded permutation)."""
+    import numpy as np
+
+    from fivonagi_gb300 import _abi
+
+    base = _abi.default_params("phased-array")
+    p = base.replace(nx=2048, ny=1024, xmax=2047 / 24, ymax=1023 / 24, center=512.0)
+    nsteps = 6000
+    rng = np.random.default_rng(args.seed)
+    targets = [(1024 + 128 * (k % 8) + 64, 128 * (k // 8) + 64) for k in rng.permutation(64)]
+    results = []
+    t_all = 0.0
+    for d in range(args.designs):
+        if d == 0:
+            _time_design(p, *_adjoint_case(p, targets[d], 200, args.seed), 200)  # warm-up
+        amp, ph, win = _adjoint_case(p, targets[d], nsteps, args.seed + 1000 + d)
+        r = _time_design(p, amp, ph, win, nsteps, fd_params=1 if d == 0 else 0)
+        t_all += r["t_fwd"] + r["t_bwd"]
+        results.append(r)
+    line = {
+        "metric": "gradients/s",
+        "value": len(results) / t_all,
+        "unit": "gradients/s",
+        "n_gpus": 1,
+        "steps": nsteps,
+        "warmup": 200,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{len(results)} phased-array designs 2048x1024, 6000 steps, 256 weights each, "
+                               "32x32 focal windows from an 8x8 grid in the right half", "seed": args.seed},
+        "adjoint_forward_ratio_mean": float(np.mean([r["t_bwd"] / r["t_plain"] for r in results])),
+        "adjoint_memory_gb_max": max(r["mem"] for r in results) / 1e9,
+        "gradient_check": results[0]["checks"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -454,9 +610,11 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU-baseline leg")
-    ap.add_argument("--workload", choices=["plain", "batched"], default="plain",
-                    help="plain: focused beam 4096x2048; batched: config-3 batch vs sequential")
+    ap.add_argument("--workload", choices=["plain", "batched", "adjoint", "designs"], default="plain",
+                    help="plain: focused beam 4096x2048; batched: config-3 batch vs sequential; "
+                         "adjoint: config-4 gradient; designs: config-5 gradients")
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--designs", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
@@ -465,6 +623,10 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
+    if args.workload == "designs":
+        return run_designs(args)
     return run_gpu(args)
 
 

@@ -437,7 +437,8 @@ struct fv_adjoint {
   float *sched = nullptr;       // dt[nsteps] then T[nsteps]
   double *acc = nullptr;        // loss sum, then gradient sums (2 nelem)
   std::vector<float> h_dt, h_T;
-  bool have_forward = false;
+  bool have_schedule = false;  // a recorded dt schedule (replays need it)
+  bool have_forward = false;   // checkpoints of the recorded run (the backward needs them)
   int exact = 1;
 };
 
@@ -678,22 +679,23 @@ fv_status fv_adjoint_forward(fv_adjoint *a, const float *amp, const float *phase
   fv_status s = set_weights(a, amp, phase);
   if (s != FV_OK) return s;
   a->have_forward = false;
+  a->have_schedule = false;
   s = run_forward(a, true, loss);
   if (s != FV_OK) return s;
   a->have_forward = true;
+  a->have_schedule = true;
   return FV_OK;
 }
 
 fv_status fv_adjoint_replay(fv_adjoint *a, const float *amp, const float *phase, double *loss) {
   if (!a || !amp || !phase) return afail(FV_BAD_ARG, "NULL argument");
-  if (!a->have_forward) return afail(FV_BAD_ARG, "no forward run: its dt schedule is replayed");
+  if (!a->have_schedule) return afail(FV_BAD_ARG, "no forward run: its dt schedule is replayed");
   fv_status s = set_weights(a, amp, phase);
   if (s != FV_OK) return s;
-  s = run_forward(a, false, loss);
-  // the recorded run's weights stay in force for the backward pass only if
-  // the caller passes them again to fv_adjoint_forward
-  if (s == FV_OK) a->have_forward = false;
-  return s;
+  // the replay overwrites the weights and the state the backward pass
+  // would differentiate: a backward needs a new fv_adjoint_forward
+  a->have_forward = false;
+  return run_forward(a, false, loss);
 }
 
 fv_status fv_adjoint_schedule(fv_adjoint *a, double *dt, double *T) {

@@ -106,3 +106,18 @@ def test_torch_function_returns_the_adjoint_gradients():
     np.testing.assert_allclose(ta.grad.numpy(), np.float32(3.0 * ga), rtol=1e-6)
     np.testing.assert_allclose(tp.grad.numpy(), np.float32(3.0 * gp), rtol=1e-6)
     adj.close()
+
+
+def test_replays_repeat_and_backward_needs_a_new_forward():
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 2, p.ampl)
+    adj = Adjoint(p, loss_window(*WIN), NSTEPS)
+    adj.forward(amp, ph)
+    l1 = adj.replay(amp * 1.01, ph)
+    l2 = adj.replay(amp * 1.01, ph)
+    assert l1 == l2
+    with pytest.raises(Exception):
+        adj.backward()
+    adj.forward(amp, ph)
+    adj.backward()
+    adj.close()
