@@ -217,8 +217,9 @@ def run_gpu(args):
     params = workload_params(exact)
     cells = params.nx * params.ny
 
-    # ---- launch shape from the autotuner (cached; outside every timed region)
-    blocks = autotune.tune(params)
+    # ---- launch shape from the autotuner (cached; outside every timed region),
+    # or as given (--blocks: few launches before a profiler's capture)
+    blocks = args.blocks if args.blocks > 0 else autotune.tune(params)
 
     # ---- device-timed throughput (state resident in HBM)
     sim = Simulation(params)
@@ -615,6 +616,8 @@ def main():
                          "adjoint: config-4 gradient; designs: config-5 gradients")
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--designs", type=int, default=32)
+    ap.add_argument("--blocks", type=int, default=0,
+                    help="plain workload: CTAs per step launch instead of the autotuner's choice")
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -135,6 +135,32 @@ class FvLossWindow(C.Structure):
     ]
 
 
+class FvCollectSpec(C.Structure):
+    _fields_ = [
+        ("nprobes", C.c_int32),
+        ("probe_i", C.c_int32 * 8),
+        ("probe_j", C.c_int32 * 8),
+        ("envelope_row", C.c_int32),
+        ("envelope_len", C.c_int32),
+        ("capacity", C.c_int32),
+        ("envelope_halfwidth", C.c_double),
+    ]
+
+
+class FvRenderSpec(C.Structure):
+    _fields_ = [
+        ("i0", C.c_int32),
+        ("j0", C.c_int32),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("zoom", C.c_int32),
+        ("jcut", C.c_int32),
+        ("overlays", C.c_int32),
+        ("reserved", C.c_int32),
+        ("plot_scale", C.c_double),
+    ]
+
+
 class FvStepResult(C.Structure):
     _fields_ = [
         ("accepted", C.c_int32),
@@ -172,6 +198,11 @@ PROTOTYPES = {
     "fv_adjoint_replay": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "fv_adjoint_schedule": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fv_adjoint_get_state": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "fv_filter_u1": (C.c_int, [_P, C.c_double, _P, C.c_int32]),
+    "fv_render": (C.c_int, [_P, C.POINTER(FvRenderSpec), _P, C.c_int32]),
+    "fv_collect_enable": (C.c_int, [_P, C.POINTER(FvCollectSpec)]),
+    "fv_collect_read": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "fv_snapshot": (C.c_int, [_P]),
     "fv_restore": (C.c_int, [_P]),
     "fv_set_stream": (C.c_int, [_P, _P]),

@@ -6,6 +6,8 @@
 // attempts are replayed from a captured CUDA graph, the host synchronises
 // once per call, and every error comes back as an fv_status.
 #include <cuda_runtime.h>
+#include <cufft.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <cmath>
@@ -13,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -81,6 +84,183 @@ __global__ void ctrl_scalars_kernel(Ctrl *c, float dt, float T, int n) {
   c->n = n;
 }
 
+// On-device data collection (the reference's dataCollect, apps/hifu-beam/
+// data_collect.h:6-107): after each accepted step with T > 0, the step's T
+// and CFL, u1 at the probe cells, and the running u1 maximum along a lab
+// row. One CTA; the control block says whether the attempt was accepted
+// and which step it was, so attempts after the run ended collect nothing.
+struct CollectDev {
+  int nprobes;
+  int pi[8], pj[8];
+  int env_row, env_len, capacity;
+  float halfwidth, eta;
+  float *T, *cfl, *probes, *env;
+  int *count;  // [0] steps in the series, [1] step number n of the last collected step
+};
+
+__global__ void collect_kernel(Ctrl *c, const float *u1a, const float *u1b, int nx, int ny, CollectDev d) {
+  __shared__ int go, k;
+  if (threadIdx.x == 0) {
+    const int n = c->n;
+    go = (c->status == 0 && c->last_accepted && n != d.count[1] && c->T > 0.0f) ? 1 : 0;
+    if (go) {
+      k = d.count[0];
+      if (k >= d.capacity) {
+        c->status = FV_COLLECT_OVERFLOW;  // simError 4 (data_collect.h:94)
+        go = 0;
+      } else {
+        d.count[0] = k + 1;
+        d.count[1] = n;
+      }
+    }
+  }
+  __syncthreads();
+  if (!go) return;
+  const float *u1 = c->cur ? u1b : u1a;
+  const int mdx = c->mdx, mdy = c->mdy;
+  const float T = c->T;
+  if (threadIdx.x == 0) {
+    d.T[k] = T;
+    d.cfl[k] = c->last_cfl;
+  }
+  if ((int)threadIdx.x < d.nprobes) {
+    const int p = threadIdx.x;
+    const int i = d.pi[p] - mdx, j = d.pj[p] - mdy;
+    d.probes[size_t(k) * 8 + p] = (i >= 0 && i < nx && j >= 0 && j < ny) ? u1[i + size_t(j) * nx] : 0.0f;
+  }
+  const int j = d.env_row - mdy;
+  if (d.env_row >= 0 && j >= 0 && j < ny) {
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+      const int lab = i + mdx;
+      if (lab >= d.env_len) continue;
+      // the central peak only (data_collect.h:99-102)
+      if (d.halfwidth > 0.0f && fabsf((float)lab / d.eta - T) > d.halfwidth) continue;
+      const float v = u1[i + size_t(j) * nx];
+      d.env[lab] = (v > d.env[lab]) ? v : d.env[lab];  // getmax, common/main.cu:63
+    }
+  }
+}
+
+// Spectral low-pass (the filter hook the reference leaves commented out,
+// common/filter.h:16-39, main.cu:672-708): zero the coefficients of the
+// half spectrum (NY rows of NX/2+1, row j holding wavenumber ky = j or
+// j - NY) whose wavenumber radius exceeds `radius`, and scale the rest by
+// 1/(NX NY) so that the inverse transform returns the field itself.
+__global__ void lowpass_kernel(cufftComplex *spec, int nx, int ny, float radius) {
+  const int kxn = nx / 2 + 1;
+  const long long total = (long long)kxn * ny;
+  const float scale = 1.0f / ((float)nx * (float)ny);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total; k += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(k % kxn);
+    const int row = (int)(k / kxn);
+    const int ky = row <= ny / 2 ? row : row - ny;
+    const float r2 = (float)kx * (float)kx + (float)ky * (float)ky;
+    cufftComplex c = spec[k];
+    const bool keep = r2 <= radius * radius;
+    c.x = keep ? c.x * scale : 0.0f;
+    c.y = keep ? c.y * scale : 0.0f;
+    spec[k] = c;
+  }
+}
+
+// Headless display (the reference's draw + colour map, apps/hifu-beam/
+// draw_float_cut.h:8-106, rendered to a GL bitmap there): a map of u1 over
+// a window of the grid, sampled every `zoom` cells, scaled to [0, 1] as
+// u1 / (2 PLOTSCALE AMPL) + 0.5 with the reference's guide lines, and under
+// it a 128-pixel plot of u1 along row jcut; then a hue/lightness colour map
+// to RGBA8.
+struct RenderArgs {
+  const float *u1;
+  int nx, ny, mdx;
+  int i0, j0, width, height, zoom, jcut, overlays;
+  float scale;        // 1 / (PLOTSCALE * AMPL)
+  int focal_i;        // ISPF (lab column), -1: none
+  int aperture_j;     // ISPa * ETA, -1: none
+  uint8_t *rgba;
+};
+
+// HLS to RGB, one channel (Foley, van Dam, Feiner, Hughes, "Computer
+// Graphics: Principles and Practice", 2nd ed., sec. 13.3.5).
+__device__ __forceinline__ uint8_t hls_channel(float n1, float n2, int hue) {
+  hue = ((hue % 360) + 360) % 360;
+  float v;
+  if (hue < 60) v = n1 + (n2 - n1) * (float)hue / 60.0f;
+  else if (hue < 180) v = n2;
+  else if (hue < 240) v = n1 + (n2 - n1) * (float)(240 - hue) / 60.0f;
+  else v = n1;
+  return (uint8_t)(255.0f * v);
+}
+
+__global__ void render_kernel(RenderArgs r) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int rows = r.height + (r.jcut >= 0 ? 128 : 0);
+  if (x >= r.width || y >= rows) return;
+  auto at = [&](int i, int j) {
+    i = min(max(i, 0), r.nx - 1);  // clamp addressing, as the texture reads
+    j = min(max(j, 0), r.ny - 1);
+    return r.u1[i + size_t(j) * r.nx];
+  };
+  const int iread = x * r.zoom + r.i0;
+  float l;
+  if (y < r.height) {
+    const int jread = y * r.zoom + r.j0;
+    l = fminf(fmaxf(at(iread, jread) * r.scale * 0.5f + 0.5f, 0.0f), 1.0f);
+    if (r.overlays) {
+      if (r.jcut >= 0 && abs(jread - r.jcut) <= r.zoom - 1) l = (iread % 40 < 20) ? 1.0f : 0.0f;
+      if (r.focal_i >= 0 && abs(iread - (r.focal_i - r.mdx)) <= r.zoom - 1) l = (jread % 40 < 20) ? 1.0f : 0.0f;
+      if (abs(x - r.width / 2) <= 1) l = 0.7f;
+      if (r.aperture_j >= 0 && abs(jread - r.aperture_j) <= 1) l = 0.7f;
+    }
+  } else {
+    // the cut plot: the curve, the zero line and the +-AMPL*PLOTSCALE lines
+    const float d = at(iread, r.jcut) * r.scale * 0.25f;
+    const int yy = y - r.height;
+    if (fabsf((float)yy - 64.0f - d * 128.0f) < 1.0f) l = 1.0f;
+    else if (yy == 64) l = 0.5f;
+    else if (yy == 96 || yy == 32) l = 0.25f;
+    else l = 0.0f;
+  }
+  // lightness l, saturation 1, hue (180 + 360 l) mod 360
+  const int hue = (180 + (int)(360.0f * l)) % 360;
+  const float m2 = l <= 0.5f ? l * 2.0f : 1.0f;
+  const float m1 = 2.0f * l - m2;
+  uint8_t *px = r.rgba + 4 * (size_t(y) * r.width + x);
+  px[0] = hls_channel(m1, m2, hue + 120);
+  px[1] = hls_channel(m1, m2, hue);
+  px[2] = hls_channel(m1, m2, hue - 120);
+  px[3] = 255;
+}
+
+// cuFFT, opened on first use so that the library itself does not depend on
+// it.
+struct CufftApi {
+  bool tried = false, ok = false;
+  cufftResult (*plan2d)(cufftHandle *, int, int, cufftType) = nullptr;
+  cufftResult (*set_stream)(cufftHandle, cudaStream_t) = nullptr;
+  cufftResult (*exec_r2c)(cufftHandle, cufftReal *, cufftComplex *) = nullptr;
+  cufftResult (*exec_c2r)(cufftHandle, cufftComplex *, cufftReal *) = nullptr;
+  cufftResult (*destroy)(cufftHandle) = nullptr;
+};
+
+CufftApi &cufft_api() {
+  static CufftApi api;
+  static std::mutex m;
+  std::lock_guard<std::mutex> lock(m);
+  if (api.tried) return api;
+  api.tried = true;
+  void *lib = dlopen("libcufft.so.12", RTLD_NOW | RTLD_LOCAL);
+  if (!lib) lib = dlopen("libcufft.so", RTLD_NOW | RTLD_LOCAL);
+  if (!lib) return api;
+  api.plan2d = reinterpret_cast<decltype(api.plan2d)>(dlsym(lib, "cufftPlan2d"));
+  api.set_stream = reinterpret_cast<decltype(api.set_stream)>(dlsym(lib, "cufftSetStream"));
+  api.exec_r2c = reinterpret_cast<decltype(api.exec_r2c)>(dlsym(lib, "cufftExecR2C"));
+  api.exec_c2r = reinterpret_cast<decltype(api.exec_c2r)>(dlsym(lib, "cufftExecC2R"));
+  api.destroy = reinterpret_cast<decltype(api.destroy)>(dlsym(lib, "cufftDestroy"));
+  api.ok = api.plan2d && api.set_stream && api.exec_r2c && api.exec_c2r && api.destroy;
+  return api;
+}
+
 }  // namespace
 
 namespace fvgb {
@@ -101,6 +281,9 @@ struct fv_handle {
   float *partials = nullptr;
   uint32_t *fix = nullptr;      // fix-up scratch of the step launches
   float *weights = nullptr;     // phased array: amplitudes then phases (device)
+  bool collect = false;         // data collection on
+  CollectDev coll{};            // its device buffers and spec
+  float *coll_mem = nullptr;
   float *snap_mem = nullptr;    // fv_snapshot: one state (3 fields)
   Ctrl *snap_ctrl = nullptr;    // fv_snapshot: the control block
   int snap_cur = -1;            // buffer the snapshot was taken from; -1: none
@@ -119,6 +302,17 @@ namespace {
 int launch(fv_handle *h, int stage, const StepArgs &a) {
   return h->exact ? launch_step_exact(a, h->warps, stage, h->stream)
                   : launch_step_fast(a, h->warps, stage, h->stream);
+}
+
+// One attempt of the run: the step's launches, then the collector if on.
+int launch_attempt(fv_handle *h) {
+  int rc = launch(h, -1, h->args);
+  if (rc == 0 && h->collect) {
+    collect_kernel<<<1, 1024, 0, h->stream>>>(h->ctrl, h->args.state[0][0], h->args.state[1][0], h->params.nx,
+                                              h->params.ny, h->coll);
+    rc = (int)cudaGetLastError();
+  }
+  return rc;
 }
 
 fv_status validate(const fv_params *p) {
@@ -259,7 +453,7 @@ fv_status ensure_graph(fv_handle *h) {
   cudaGraph_t g = nullptr;
   FV_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   int rc = 0;
-  for (int k = 0; k < kGraphAttempts && rc == 0; ++k) rc = launch(h, -1, h->args);
+  for (int k = 0; k < kGraphAttempts && rc == 0; ++k) rc = launch_attempt(h);
   cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
   if (rc != 0) return fail(FV_CUDA_ERROR, "step launch during capture: %s", cudaGetErrorString((cudaError_t)rc));
   if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
@@ -283,7 +477,7 @@ fv_status enqueue_attempts(fv_handle *h, long long n) {
     }
   }
   for (long long k = 0; k < n; ++k) {
-    int rc = launch(h, -1, h->args);
+    int rc = launch_attempt(h);
     if (rc != 0) return fail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
   }
   return FV_OK;
@@ -544,6 +738,7 @@ fv_status fv_destroy(fv_handle *h) {
   if (h->partials) cudaFree(h->partials);
   if (h->fix) cudaFree(h->fix);
   if (h->weights) cudaFree(h->weights);
+  if (h->coll_mem) cudaFree(h->coll_mem);
   if (h->snap_mem) cudaFree(h->snap_mem);
   if (h->snap_ctrl) cudaFree(h->snap_ctrl);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -574,6 +769,153 @@ fv_status fv_set_state(fv_handle *h, const float *u1, const float *u2, const flo
     FV_CUDA(cudaMemcpyAsync(field_ptr(h, 0, f), src[f], h->ncell * sizeof(float), kind, h->stream));
   fv_status s = reset_ctrl(h);
   if (s != FV_OK) return s;
+  if (h->collect) {
+    const int none[2] = {0, -1};
+    FV_CUDA(cudaMemcpyAsync(h->coll.count, none, sizeof(none), cudaMemcpyHostToDevice, h->stream));
+    FV_CUDA(cudaMemsetAsync(h->coll.env, 0, size_t(h->coll.env_len) * sizeof(float), h->stream));
+  }
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  return FV_OK;
+}
+
+fv_status fv_filter_u1(fv_handle *h, double radius, float *out, int32_t on_device) {
+  if (!h || !out) return fail(FV_BAD_ARG, "NULL argument");
+  if (!(radius >= 0)) return fail(FV_BAD_ARG, "radius must be >= 0");
+  CufftApi &api = cufft_api();
+  if (!api.ok) return fail(FV_CUDA_ERROR, "cuFFT (libcufft.so.12) could not be loaded");
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  const int nx = h->params.nx, ny = h->params.ny;
+  const size_t ncomplex = size_t(nx / 2 + 1) * size_t(ny);
+  // the half spectrum, then the filtered field in a buffer of its own (an
+  // in-place inverse would write rows padded to 2 (NX/2 + 1) floats)
+  void *buf = nullptr;
+  FV_CUDA(cudaMalloc(&buf, ncomplex * sizeof(cufftComplex) + h->ncell * sizeof(float)));
+  cufftReal *field = reinterpret_cast<cufftReal *>(static_cast<cufftComplex *>(buf) + ncomplex);
+  cufftHandle fwd = 0, inv = 0;
+  auto done = [&](fv_status st) {
+    if (fwd) api.destroy(fwd);
+    if (inv) api.destroy(inv);
+    cudaFree(buf);
+    return st;
+  };
+  // rows of NX floats, i fastest: the plan's dimensions are (NY, NX)
+  if (api.plan2d(&fwd, ny, nx, CUFFT_R2C) != CUFFT_SUCCESS || api.plan2d(&inv, ny, nx, CUFFT_C2R) != CUFFT_SUCCESS)
+    return done(fail(FV_CUDA_ERROR, "cufftPlan2d failed"));
+  api.set_stream(fwd, h->stream);
+  api.set_stream(inv, h->stream);
+  cufftComplex *spec = static_cast<cufftComplex *>(buf);
+  if (api.exec_r2c(fwd, field_ptr(h, h->ctrl_host->cur, 0), spec) != CUFFT_SUCCESS)
+    return done(fail(FV_CUDA_ERROR, "cufftExecR2C failed"));
+  lowpass_kernel<<<4 * 152, 256, 0, h->stream>>>(spec, nx, ny, float(radius));
+  if (api.exec_c2r(inv, spec, field) != CUFFT_SUCCESS)
+    return done(fail(FV_CUDA_ERROR, "cufftExecC2R failed"));
+  cudaError_t e = cudaMemcpyAsync(out, field, h->ncell * sizeof(float),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return done(fail(FV_CUDA_ERROR, "filter: %s", cudaGetErrorString(e)));
+  return done(FV_OK);
+}
+
+fv_status fv_render(fv_handle *h, const fv_render_spec *spec, uint8_t *rgba, int32_t on_device) {
+  if (!h || !spec || !rgba) return fail(FV_BAD_ARG, "NULL argument");
+  if (spec->width < 1 || spec->height < 1 || spec->zoom < 1 || spec->width > 16384 || spec->height > 16384)
+    return fail(FV_BAD_ARG, "render size must be 1..16384 pixels and zoom >= 1");
+  if (!(spec->plot_scale > 0)) return fail(FV_BAD_ARG, "plot_scale must be positive");
+  fv_status s = read_ctrl(h);
+  if (s != FV_OK) return s;
+  const Ctrl &c = *h->ctrl_host;
+  RenderArgs r{};
+  r.u1 = field_ptr(h, c.cur, 0);
+  r.nx = h->params.nx;
+  r.ny = h->params.ny;
+  r.mdx = c.mdx;
+  r.i0 = spec->i0;
+  r.j0 = spec->j0;
+  r.width = spec->width;
+  r.height = spec->height;
+  r.zoom = spec->zoom;
+  r.jcut = spec->jcut;
+  r.overlays = spec->overlays;
+  r.scale = float(1.0 / (spec->plot_scale * h->params.ampl));
+  r.focal_i = h->params.app == FV_APP_HIFU_BEAM ? int(h->dp.ispf) : -1;
+  r.aperture_j = h->params.app == FV_APP_HIFU_BEAM ? int(h->dp.ispa * (float(h->params.nx) / float(h->params.xmax))) : -1;
+  const int rows = spec->height + (spec->jcut >= 0 ? 128 : 0);
+  const size_t bytes = size_t(spec->width) * size_t(rows) * 4;
+  uint8_t *dev = rgba;
+  if (!on_device) FV_CUDA(cudaMalloc(&dev, bytes));
+  r.rgba = dev;
+  const dim3 blk(32, 8), grd((spec->width + 31) / 32, (rows + 7) / 8);
+  render_kernel<<<grd, blk, 0, h->stream>>>(r);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(rgba, dev, bytes, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (!on_device) cudaFree(dev);
+  if (e != cudaSuccess) return fail(FV_CUDA_ERROR, "render: %s", cudaGetErrorString(e));
+  return FV_OK;
+}
+
+fv_status fv_collect_enable(fv_handle *h, const fv_collect_spec *spec) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  if (h->coll_mem) cudaFree(h->coll_mem);
+  h->coll_mem = nullptr;
+  h->collect = false;
+  h->coll = CollectDev{};
+  if (!spec) return FV_OK;
+  if (spec->nprobes < 0 || spec->nprobes > 8) return fail(FV_BAD_ARG, "nprobes must be 0..8");
+  if (spec->capacity < 1 || spec->capacity > (1 << 24)) return fail(FV_BAD_ARG, "capacity must be 1..2^24");
+  if (spec->envelope_row >= 0 && (spec->envelope_len < 1 || spec->envelope_len > (1 << 26)))
+    return fail(FV_BAD_ARG, "envelope_len must be 1..2^26");
+  CollectDev d{};
+  d.nprobes = spec->nprobes;
+  for (int p = 0; p < 8; ++p) {
+    d.pi[p] = spec->probe_i[p];
+    d.pj[p] = spec->probe_j[p];
+  }
+  d.env_row = spec->envelope_row;
+  d.env_len = spec->envelope_row >= 0 ? spec->envelope_len : 0;
+  d.capacity = spec->capacity;
+  d.halfwidth = float(spec->envelope_halfwidth);
+  d.eta = float(h->params.nx) / float(h->params.xmax);  // ETA = NX/XMAX (hifu parameters.h:30)
+  const size_t cap = size_t(d.capacity);
+  const size_t floats = cap * 2 + cap * 8 + size_t(d.env_len) + 2;
+  FV_CUDA(cudaMalloc(&h->coll_mem, floats * sizeof(float)));
+  d.T = h->coll_mem;
+  d.cfl = d.T + cap;
+  d.probes = d.cfl + cap;
+  d.env = d.probes + cap * 8;
+  d.count = reinterpret_cast<int *>(d.env + d.env_len);
+  FV_CUDA(cudaMemsetAsync(h->coll_mem, 0, floats * sizeof(float), h->stream));
+  const int none[2] = {0, -1};
+  FV_CUDA(cudaMemcpyAsync(d.count, none, sizeof(none), cudaMemcpyHostToDevice, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  h->coll = d;
+  h->collect = true;
+  return FV_OK;
+}
+
+fv_status fv_collect_read(fv_handle *h, int32_t *nsteps, float *T, float *cfl, float *probes,
+                          float *envelope) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (!h->collect) return fail(FV_BAD_ARG, "collection is off (fv_collect_enable)");
+  const CollectDev &d = h->coll;
+  int count[2] = {0, -1};
+  FV_CUDA(cudaMemcpyAsync(count, d.count, sizeof(count), cudaMemcpyDeviceToHost, h->stream));
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  const size_t k = size_t(count[0]);
+  if (nsteps) *nsteps = count[0];
+  if (T && k) FV_CUDA(cudaMemcpy(T, d.T, k * sizeof(float), cudaMemcpyDeviceToHost));
+  if (cfl && k) FV_CUDA(cudaMemcpy(cfl, d.cfl, k * sizeof(float), cudaMemcpyDeviceToHost));
+  if (probes && k) FV_CUDA(cudaMemcpy(probes, d.probes, k * 8 * sizeof(float), cudaMemcpyDeviceToHost));
+  if (envelope && d.env_len)
+    FV_CUDA(cudaMemcpy(envelope, d.env, size_t(d.env_len) * sizeof(float), cudaMemcpyDeviceToHost));
+  // empty the series for the next frame; the last collected step stays
+  FV_CUDA(cudaMemsetAsync(d.count, 0, sizeof(int), h->stream));
   FV_CUDA(cudaStreamSynchronize(h->stream));
   return FV_OK;
 }

@@ -57,7 +57,7 @@ struct Ctrl {
   int64_t accepted;       // counters since the last fv_run/fv_sync reset
   int64_t rejected;
   uint32_t blocks_done;   // unused (zero)
-  uint32_t pad;
+  int32_t last_accepted;  // the last decided attempt was accepted (1) or rejected (0)
 };
 
 // Ghost frame: the boundary hook's values of the ghost cells (the two

@@ -393,6 +393,7 @@ __device__ void decide(volatile Ctrl *vc, const DevParams &p, float cfl, bool ne
   if (negative) {
     vc->status = FV_NEGATIVE_EIGENVALUE;
     vc->neg_flag = 0;
+    vc->last_accepted = 0;
     return;
   }
   int sim_error = 0;
@@ -417,6 +418,7 @@ __device__ void decide(volatile Ctrl *vc, const DevParams &p, float cfl, bool ne
     if (cr >= p.max_retries) vc->status = FV_DT_TOO_LARGE;
   }
   vc->sim_error = sim_error;
+  vc->last_accepted = sim_error ? 0 : 1;
   // update_dt, main.cu:214-230 (the 0.9 is a double literal)
   const float new_dt = dt * p.cflwhish / cfl;
   if (sim_error == 1 && (double)new_dt > (double)dt * 0.9)
@@ -637,8 +639,10 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
 
 // Decides the attempt after the step and fix-up launches: one CTA, so no
 // CTA of the wide launches has to count who finishes last.
-__global__ void __launch_bounds__(kThreads) finalize_kernel(StepArgs a) {
-  __shared__ float red[kWarps];
+constexpr int kFinalizeThreads = 1024;  // one CTA; enough threads that the partials take one or two loads each
+
+__global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs a) {
+  __shared__ float red[kFinalizeThreads / 32];
   if (!attempt_active(a.ctrl)) return;
   finalize(a, red);
 }
@@ -906,7 +910,7 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
     case -1:
       step_kernel<-1><<<grid, block, 0, st>>>(a);
       fixup_kernel<<<a.fix_blocks, block, 0, st>>>(a);
-      finalize_kernel<<<1, block, 0, st>>>(a);
+      finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;
     case 0: step_kernel<0><<<grid, block, 0, st>>>(a); break;
     case 1: step_kernel<1><<<grid, block, 0, st>>>(a); break;

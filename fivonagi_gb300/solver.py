@@ -92,6 +92,62 @@ class Simulation:
         check(self.lib.fv_set_array_weights(self.h, a.ctypes.data_as(fp), ph.ctypes.data_as(fp), int(a.size)),
               "fv_set_array_weights")
 
+    def filter_u1(self, radius: float) -> np.ndarray:
+        """The current u1 low-pass filtered in Fourier space (fv_filter_u1)."""
+        out = np.empty(self.shape, np.float32)
+        check(self.lib.fv_filter_u1(self.h, float(radius), out.ctypes.data, 0), "fv_filter_u1")
+        return out
+
+    def render(self, width=None, height=None, zoom: int = 1, i0: int = 0, j0: int = 0, jcut: int = -1,
+               overlays: bool = False, plot_scale: float = 1.0) -> np.ndarray:
+        """The headless display (fv_render): an RGBA8 image, rows first."""
+        spec = _abi.FvRenderSpec()
+        spec.width = int(width or self.params.nx // zoom)
+        spec.height = int(height or self.params.ny // zoom)
+        spec.zoom, spec.i0, spec.j0, spec.jcut = int(zoom), int(i0), int(j0), int(jcut)
+        spec.overlays, spec.plot_scale = int(bool(overlays)), float(plot_scale)
+        rows = spec.height + (128 if jcut >= 0 else 0)
+        out = np.zeros((rows, spec.width, 4), np.uint8)
+        check(self.lib.fv_render(self.h, C.byref(spec), out.ctypes.data, 0), "fv_render")
+        return out
+
+    def collect_enable(self, probes=(), envelope_row: int = -1, envelope_len: int = 0, capacity: int = 0,
+                       envelope_halfwidth: float = 0.0) -> None:
+        """On-device collection after each accepted step (fv_collect_enable):
+        probes = [(i_lab, j_lab), ...] (at most 8); the u1 envelope along lab
+        row envelope_row; capacity steps between reads (default NX)."""
+        spec = _abi.FvCollectSpec()
+        spec.nprobes = len(probes)
+        for k, (i, j) in enumerate(probes):
+            spec.probe_i[k], spec.probe_j[k] = int(i), int(j)
+        spec.envelope_row = int(envelope_row)
+        spec.envelope_len = int(envelope_len or self.params.nx)
+        spec.capacity = int(capacity or self.params.nx)
+        spec.envelope_halfwidth = float(envelope_halfwidth)
+        self._collect = spec
+        check(self.lib.fv_collect_enable(self.h, C.byref(spec)), "fv_collect_enable")
+
+    def collect_disable(self) -> None:
+        check(self.lib.fv_collect_enable(self.h, None), "fv_collect_enable")
+        self._collect = None
+
+    def collect_read(self) -> dict:
+        """The series since the last read (T, cfl, probes [steps, nprobes])
+        and the envelope; empties the series."""
+        spec = self._collect
+        cap = spec.capacity
+        T = np.zeros(cap, np.float32)
+        cfl = np.zeros(cap, np.float32)
+        probes = np.zeros((cap, 8), np.float32)
+        env = np.zeros(max(spec.envelope_len, 1), np.float32)
+        n = C.c_int32()
+        fp = C.POINTER(C.c_float)
+        check(self.lib.fv_collect_read(self.h, C.byref(n), T.ctypes.data_as(fp), cfl.ctypes.data_as(fp),
+                                       probes.ctypes.data_as(fp), env.ctypes.data_as(fp)), "fv_collect_read")
+        k = n.value
+        return {"steps": k, "T": T[:k], "cfl": cfl[:k], "probes": probes[:k, :spec.nprobes],
+                "envelope": env[:spec.envelope_len] if spec.envelope_row >= 0 else None}
+
     def snapshot(self) -> None:
         """Save the state and time-stepping scalars (one slot)."""
         check(self.lib.fv_snapshot(self.h), "fv_snapshot")

@@ -39,7 +39,7 @@ typedef enum fv_status {
   FV_DT_TOO_LARGE = 1,        /* CFL >= CFLMAX on every retry of a step (max_retries) */
   FV_NEGATIVE_EIGENVALUE = 2, /* a Riemann solve met tmp3 < 0 (apps/na/fv.h:102, 290) */
   FV_TRANSONIC = 3,           /* declared by the reference, never raised; reserved */
-  FV_COLLECT_OVERFLOW = 4,    /* reserved for data collection */
+  FV_COLLECT_OVERFLOW = 4,    /* the collection buffers filled before fv_collect_read (simError 4) */
   FV_TIMEOUT = 5,             /* a bounded device wait ran out */
   FV_CUDA_ERROR = 6,          /* a CUDA runtime call failed; see fv_last_error_string */
   FV_BAD_ARG = 7,             /* invalid argument; see fv_last_error_string */
@@ -190,6 +190,63 @@ fv_status fv_adjoint_replay(fv_adjoint *a, const float *amp, const float *phase,
 fv_status fv_adjoint_schedule(fv_adjoint *a, double *dt, double *T);
 /* The state after the last forward or replay (host buffers of NX*NY floats). */
 fv_status fv_adjoint_get_state(fv_adjoint *a, float *u1, float *u2, float *u3);
+
+/* Spectral low-pass of the current u1 (the filter the reference sketches in
+ * common/filter.h:16-39 and main.cu:672-708 but never runs): a 2-D real FFT
+ * (cuFFT, loaded at first use), every coefficient with wavenumber radius
+ * sqrt(kx^2 + ky^2) > radius zeroed (kx, ky in index units, ky folded to
+ * -NY/2..NY/2), the inverse FFT normalised by NX*NY. Writes NX*NY floats
+ * to `out` (host, or device with on_device = 1); the state is unchanged. */
+fv_status fv_filter_u1(fv_handle *h, double radius, float *out, int32_t on_device);
+
+/* Headless display: the reference's draw kernel and colour map (apps/
+ * hifu-beam/draw_float_cut.h:8-106), rendered into an RGBA8 buffer instead
+ * of a GL window. A width x height map of u1 over the cells
+ * (i0 + x*zoom, j0 + y*zoom) (NXWLB, NYWLB, NXW/ZOOM, NYW/ZOOM, ZOOM),
+ * coloured from u1/(2 plot_scale AMPL) + 0.5, with the reference's guide
+ * lines when overlays = 1; with jcut >= 0, a 128-pixel plot of u1 along
+ * row jcut under it. Writes width * (height [+ 128]) pixels, row 0 first,
+ * to `rgba` (host, or device with on_device = 1). */
+typedef struct fv_render_spec {
+  int32_t i0, j0;          /* first cell of the view */
+  int32_t width, height;   /* map size, pixels */
+  int32_t zoom;            /* cells per pixel */
+  int32_t jcut;            /* row of the cut plot; -1: none */
+  int32_t overlays;        /* 1: dashed cut row and focal column, centre and aperture lines */
+  int32_t reserved;
+  double plot_scale;       /* PLOTSCALE: full colour range is +-plot_scale*AMPL */
+} fv_render_spec;
+fv_status fv_render(fv_handle *h, const fv_render_spec *spec, uint8_t *rgba, int32_t on_device);
+
+/* ------------------------------------------------------- data collection
+ * On-device collection after every accepted step with T > 0, the
+ * reference's dataCollect (apps/hifu-beam/data_collect.h:6-107,
+ * apps/taylor-angle-xy/data_collect.h:6-98), read back between frames:
+ *  - T and the step's CFL, one entry per step (measure1 rows 0, 1);
+ *  - u1 at up to 8 probe cells ("microphones", rows 2-5), in lab
+ *    coordinates (i + MDX, j + MDY); 0 while a probe is outside the window;
+ *  - the running maximum of u1 along lab row envelope_row (u1max, row 6),
+ *    over lab columns 0..envelope_len-1, only where |x_lab/ETA - T| <=
+ *    envelope_halfwidth when that is > 0 (ETA = NX/XMAX; the hifu app's
+ *    central-peak window is 0.5).
+ * The per-step series hold `capacity` steps; a step beyond that stops the
+ * run with FV_COLLECT_OVERFLOW, as simError 4 does. fv_collect_read copies
+ * the series out (host buffers: T, cfl [capacity], probes [capacity][8],
+ * envelope [envelope_len]; any may be NULL), returns the step count and
+ * empties the series; the envelope keeps accumulating. A NULL spec turns
+ * collection off. Setting the state clears everything. */
+typedef struct fv_collect_spec {
+  int32_t nprobes;             /* 0..8 */
+  int32_t probe_i[8];          /* lab column of each probe */
+  int32_t probe_j[8];          /* lab row of each probe */
+  int32_t envelope_row;        /* lab row of the u1 envelope; -1: none */
+  int32_t envelope_len;        /* lab columns of the envelope */
+  int32_t capacity;            /* steps the series hold between reads (>= 1) */
+  double envelope_halfwidth;   /* > 0: central-peak window, in units of x/ETA - T */
+} fv_collect_spec;
+fv_status fv_collect_enable(fv_handle *h, const fv_collect_spec *spec);
+fv_status fv_collect_read(fv_handle *h, int32_t *nsteps, float *T, float *cfl, float *probes,
+                          float *envelope);
 
 /* Save the current state and time-stepping scalars (dt, T, n, window
  * offsets, retry state) in the handle's one snapshot slot, overwriting it;
