@@ -6,7 +6,7 @@ Translation units, compiled in parallel:
   fv_api.cu           the C ABI of one simulation (host code, control-block kernels)
   fv_batch.cu         the C ABI of batches
   fv_noalloc.cu       one step attempt with no device allocation
-  fv_adjoint.cu       --fmad=false: the adjoint's reverse kernels recompute the exact forward
+  fv_adjoint.cu       the adjoint (its forward runs the step kernels above)
 """
 from __future__ import annotations
 
@@ -42,7 +42,7 @@ def _units():
         ("fv_api.o", os.path.join(CSRC, "fv_api.cu"), []),
         ("fv_batch.o", os.path.join(CSRC, "fv_batch.cu"), []),
         ("fv_noalloc.o", os.path.join(CSRC, "fv_noalloc.cu"), []),
-        ("fv_adjoint.o", os.path.join(CSRC, "fv_adjoint.cu"), ["--fmad=false"]),
+        ("fv_adjoint.o", os.path.join(CSRC, "fv_adjoint.cu"), []),
     ]
 
 

@@ -2,9 +2,9 @@
 // element weights.
 //
 // The reference has no adjoint. This is the reverse mode of this library's
-// own forward step (the same FP32 operations, recomputed with IEEE
-// division, which the forward reproduces bit for bit), differentiated with
-// the dt schedule of a base forward run held fixed:
+// own forward step, differentiated at the forward's own states (recorded
+// during the segment replays) with the dt schedule of a base forward run
+// held fixed:
 //
 //   u_n = S(u_{n-1}; weights, dt_{n-1}, T_{n-1}),   S = D o X o Y o B
 //
@@ -19,12 +19,14 @@
 // step's window sum to the loss -- all device-side, no host round trip per
 // step. Backward: segment by segment from the last checkpoint, replay the
 // segment's steps from its checkpoint (frozen dt) into a buffer of C
-// states, then walk the segment backwards. A reverse step recomputes the
-// forward stages B, Y, X of its input in one stage-kernel pass and runs
-// grid-wide reverse kernels: diffusion, x sweep, y sweep (three kernels
-// each: waves, interface adjoints, per-cell gather), boundary (ghost cells
-// back to the cells they copy, and the source cells to the weights).
-// Memory: (N / C + C + ~30) grids; C = ceil(sqrt(N)) by default.
+// states; each replayed attempt also records its stage grids B, Y, X (the
+// step kernel writes them as it goes, kStageRecord), the linearisation
+// points of the reverse step. Then walk the segment backwards. A reverse
+// step runs grid-wide reverse kernels: diffusion, x sweep, y sweep (three
+// kernels each: waves, interface adjoints, per-cell gather), boundary
+// (ghost cells back to the cells they copy, and the source cells to the
+// weights).
+// Memory: 3 (N / C) + 12 C + ~40 grids; C = ceil(sqrt(N)) by default.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -205,10 +207,10 @@ __global__ void adj_diffusion_kernel(DevParams p, float dt, CG3 s2, CG3 lo, G3 l
     gvy += c * lo.f[2][q];
   }
   const float rho = s2.f[0][o] + 1.0f;
-  const float vx = s2.f[1][o] / rho, vy = s2.f[2][o] / rho;
-  li.f[0][o] = lo.f[0][o] - (gvx * vx + gvy * vy) / rho;
-  li.f[1][o] = lo.f[1][o] + gvx / rho;
-  li.f[2][o] = lo.f[2][o] + gvy / rho;
+  const float vx = fdiv(s2.f[1][o], rho), vy = fdiv(s2.f[2][o], rho);
+  li.f[0][o] = lo.f[0][o] - fdiv(gvx * vx + gvy * vy, rho);
+  li.f[1][o] = lo.f[1][o] + fdiv(gvx, rho);
+  li.f[2][o] = lo.f[2][o] + fdiv(gvy, rho);
 }
 
 // Local frame of a sweep: component 1 = u1; x sweep (dir 0): normal = u2,
@@ -247,9 +249,9 @@ __global__ void adj_waves_kernel(DevParams p, int dir, float dt, CG3 s, WaveStor
     const float dtx = dt / (dir == 0 ? p.dx : p.dy);
     float cfl = 0.0f;
     Fluct f;
-    DivIEEE ieee;
-    riemann(ra, qna, qta, qna / ra, qta / ra, rb, qnb, qtb, qnb / rb, qtb / rb, 2.0f * (p.beta - 1.0f), dtx,
-            cfl, w, f, ieee);
+    DivFast fast;
+    riemann(ra, qna, qta, fdiv(qna, ra), fdiv(qta, ra), rb, qnb, qtb, fdiv(qnb, rb), fdiv(qtb, rb),
+            2.0f * (p.beta - 1.0f), dtx, cfl, w, f, fast);
   }
   ws.w[0][o] = w.s1; ws.w[1][o] = w.s2; ws.w[2][o] = w.s3;
   ws.w[3][o] = w.w11; ws.w[4][o] = w.w21; ws.w[5][o] = w.w31;
@@ -421,7 +423,7 @@ struct fv_adjoint {
   float *state[2][3] = {};      // forward state pair
   float *ckpt = nullptr;        // nckpt states
   float *seg = nullptr;         // C + 1 states of the segment being reversed
-  float *stage[3][3] = {};      // B, S1, S2 of the reverse step
+  float *stg = nullptr;         // C stage triples (B, S1, S2) of the segment's steps
   float *lam[2][3] = {};        // adjoint ping-pong
   float *tmp[2][3] = {};        // sweep adjoints
   float *waves[10] = {};
@@ -439,6 +441,8 @@ struct fv_adjoint {
   std::vector<float> h_dt, h_T;
   bool have_schedule = false;  // a recorded dt schedule (replays need it)
   bool have_forward = false;   // checkpoints of the recorded run (the backward needs them)
+  int final_cur = 0;           // state[final_cur] holds the last forward's final state
+                               // (the backward's replays reuse the control block)
   int exact = 1;
 };
 
@@ -471,6 +475,10 @@ G3 g3(float *const f[3]) { return G3{{f[0], f[1], f[2]}}; }
 CG3 cg3(float *const f[3]) { return CG3{{f[0], f[1], f[2]}}; }
 
 float *slot(float *base, size_t stride, long long k, int f) { return base + (size_t(k) * 3 + f) * stride; }
+// grid f of stage st (0 = B, 1 = S1, 2 = S2) of the segment's k-th step
+float *stage_grid(const fv_adjoint *a, long long k, int st, int f) {
+  return a->stg + ((size_t(k) * 3 + st) * 3 + f) * a->stride;
+}
 
 fv_status set_weights(fv_adjoint *a, const float *amp, const float *phase) {
   const int n = a->dp.nelem;
@@ -536,6 +544,12 @@ fv_status run_forward(fv_adjoint *a, bool record, double *loss) {
     FVA_CUDA(cudaStreamSynchronize(a->stream));
     if (c.status) return afail((fv_status)c.status, "replay stopped with status %d", c.status);
   }
+  {
+    Ctrl c;
+    FVA_CUDA(cudaMemcpyAsync(&c, a->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, a->stream));
+    FVA_CUDA(cudaStreamSynchronize(a->stream));
+    a->final_cur = c.cur & 1;
+  }
   double sum = 0.0;
   FVA_CUDA(cudaMemcpy(&sum, a->acc, sizeof(double), cudaMemcpyDeviceToHost));
   const double K = double(w.step_last - w.step_first + 1), W = double(w.ni) * double(w.nj);
@@ -585,9 +599,9 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   a->dp = dev_params_of(*p);
   a->dp_replay = a->dp;
   a->dp_replay.cflmax = __builtin_huge_valf();
-  // grids: state 2x3, checkpoints, segment (C + 1 states), stage 3x3,
-  // lam 2x3, tmp 2x3, waves 10, gab 6
-  const size_t nstates = 2 + size_t(a->nckpt) + size_t(a->every + 1) + 3 + 2 + 2;
+  // grids: state 2x3, checkpoints, segment (C + 1 states), C stage
+  // triples 3x3, lam 2x3, tmp 2x3, waves 10, gab 6
+  const size_t nstates = 2 + size_t(a->nckpt) + size_t(a->every + 1) + 3 * size_t(a->every) + 2 + 2;
   const size_t ngrids = nstates * 3 + 10 + 6;
   cudaError_t e = cudaMalloc(&a->mem, ngrids * a->stride * sizeof(float));
   if (e != cudaSuccess)
@@ -605,10 +619,7 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   }
   a->ckpt = take(a->nckpt);
   a->seg = take(a->every + 1);
-  for (int k = 0; k < 3; ++k) {
-    float *base = take(1);
-    for (int f = 0; f < 3; ++f) a->stage[k][f] = base + f * a->stride;
-  }
+  a->stg = take(3 * size_t(a->every));
   for (int k = 0; k < 2; ++k) {
     float *base = take(1);
     for (int f = 0; f < 3; ++f) a->lam[k][f] = base + f * a->stride;
@@ -710,12 +721,10 @@ fv_status fv_adjoint_schedule(fv_adjoint *a, double *dt, double *T) {
 
 fv_status fv_adjoint_get_state(fv_adjoint *a, float *u1, float *u2, float *u3) {
   if (!a || !u1 || !u2 || !u3) return afail(FV_BAD_ARG, "NULL argument");
-  Ctrl c;
-  FVA_CUDA(cudaMemcpyAsync(&c, a->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, a->stream));
   FVA_CUDA(cudaStreamSynchronize(a->stream));
   float *dst[3] = {u1, u2, u3};
   for (int f = 0; f < 3; ++f)
-    FVA_CUDA(cudaMemcpy(dst[f], a->state[c.cur & 1][f], a->ncell * sizeof(float), cudaMemcpyDeviceToHost));
+    FVA_CUDA(cudaMemcpy(dst[f], a->state[a->final_cur][f], a->ncell * sizeof(float), cudaMemcpyDeviceToHost));
   return FV_OK;
 }
 
@@ -734,14 +743,9 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   // lambda_N: the loss gradient of the final state
   int lc = 0;  // lam[lc] holds lambda_n
   FVA_CUDA(cudaMemsetAsync(a->lam[lc][0], 0, bytes, a->stream));
-  {
-    Ctrl c;
-    FVA_CUDA(cudaMemcpyAsync(&c, a->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, a->stream));
-    FVA_CUDA(cudaStreamSynchronize(a->stream));
-    if (a->nsteps >= w.step_first && a->nsteps <= w.step_last)
-      adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(a->state[c.cur & 1][0], a->lam[lc][0], nx, w.i0, w.j0,
-                                                            w.ni, w.nj, coef);
-  }
+  if (a->nsteps >= w.step_first && a->nsteps <= w.step_last)
+    adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(a->state[a->final_cur][0], a->lam[lc][0], nx, w.i0,
+                                                          w.j0, w.ni, w.nj, coef);
   WaveStore ws;
   for (int k = 0; k < 10; ++k) ws.w[k] = a->waves[k];
   AdjStore as;
@@ -749,17 +753,21 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   const long long C = a->every;
   for (long long seg0 = ((a->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, a->nsteps);  // steps seg0+1 .. seg1
-    // the segment's states u_seg0 .. u_{seg1-1}: checkpoint, then replay
+    // the segment's states u_seg0 .. u_seg1 and the stage grids of steps
+    // seg0+1 .. seg1: checkpoint, then replay with stage recording
     FVA_CUDA(cudaMemcpyAsync(slot(a->seg, a->stride, 0, 0), slot(a->ckpt, a->stride, seg0 / C, 0), bytes,
                              cudaMemcpyDeviceToDevice, a->stream));
-    for (long long n = seg0 + 1; n < seg1; ++n) {
+    for (long long n = seg0 + 1; n <= seg1; ++n) {
       float *in[3], *out[3];
       for (int f = 0; f < 3; ++f) {
         in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
         out[f] = slot(a->seg, a->stride, n - seg0, f);
       }
       adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0);
-      const int rc = launch(a, step_args(a, a->dp_replay, in, out), -1);
+      StepArgs s = step_args(a, a->dp_replay, in, out);
+      for (int st = 0; st < 3; ++st)
+        for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = stage_grid(a, n - 1 - seg0, st, f);
+      const int rc = launch(a, s, kStageRecord);
       if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
     for (long long n = seg1; n > seg0; --n) {
@@ -767,26 +775,21 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
       float *in[3];
       for (int f = 0; f < 3; ++f) in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
       const float dt = a->h_dt[n - 1], T = a->h_T[n - 1];
-      adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0);
-      {
-        // boundary-applied state, y-swept and x-swept state in one pass
-        StepArgs s = step_args(a, a->dp_replay, in, in);
-        for (int st = 0; st < 3; ++st)
-          for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = a->stage[st][f];
-        const int rc = launch(a, s, kStageAll);
-        if (rc != 0) return afail(FV_CUDA_ERROR, "stage launch: %s", cudaGetErrorString((cudaError_t)rc));
-      }
+      // the recorded boundary-applied, y-swept and x-swept states
+      float *stage[3][3];
+      for (int st = 0; st < 3; ++st)
+        for (int f = 0; f < 3; ++f) stage[st][f] = stage_grid(a, n - 1 - seg0, st, f);
       float *const *lo = a->lam[lc];
       float *const *li = a->lam[lc ^ 1];
       // diffusion: lam_n -> tmp0 (adjoint of S2)
-      adj_diffusion_kernel<<<grd, blk, 0, a->stream>>>(a->dp, dt, cg3(a->stage[2]), cg3(lo), g3(a->tmp[0]));
+      adj_diffusion_kernel<<<grd, blk, 0, a->stream>>>(a->dp, dt, cg3(stage[2]), cg3(lo), g3(a->tmp[0]));
       // x sweep on S1: tmp0 -> tmp1 (adjoint of S1)
-      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(a->stage[1]), ws);
-      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(a->stage[1]), cg3(a->tmp[0]), ws, as);
+      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(stage[1]), ws);
+      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(stage[1]), cg3(a->tmp[0]), ws, as);
       adj_combine_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, cg3(a->tmp[0]), as, g3(a->tmp[1]));
       // y sweep on B: tmp1 -> tmp0 (adjoint of B)
-      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(a->stage[0]), ws);
-      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(a->stage[0]), cg3(a->tmp[1]), ws, as);
+      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(stage[0]), ws);
+      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(stage[0]), cg3(a->tmp[1]), ws, as);
       adj_combine_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, cg3(a->tmp[1]), as, g3(a->tmp[0]));
       // boundary: weights, then lam_{n-1}
       adj_weights_kernel<<<(nelem + 127) / 128, 128, 0, a->stream>>>(a->dp, T, cg3(a->tmp[0]), g_amp, g_ph);

@@ -15,6 +15,33 @@
 
 namespace fvgb {
 
+// Division of the reverse pass: PTX div.full.f32, a full-range quotient
+// within 2 ulp, without the operand-dependent slow path of IEEE division.
+// The reverse kernels use the forward values only as the point where the
+// step is linearised. The branches they replay (signs of wave speeds,
+// limiter branches) can differ from the forward's only where a value lies
+// within a few ulps of the branch point, and there both branches give
+// nearly the same derivative.
+__device__ __forceinline__ float fdiv(float a, float b) {
+  float q;
+  asm("div.full.f32 %0, %1, %2;" : "=f"(q) : "f"(a), "f"(b));
+  return q;
+}
+
+// The division policy of fv_device.cuh's riemann() and mc_limit() for
+// the reverse pass's recomputation: fdiv everywhere.
+struct DivFast {
+  static constexpr bool kFlags = false;
+  struct Rcp {
+    float b;
+  };
+  __device__ __forceinline__ Rcp recip(float b) { return Rcp{b}; }
+  __device__ __forceinline__ float div_r(float a, const Rcp &rb) { return fdiv(a, rb.b); }
+  __device__ __forceinline__ float div(float a, float b) { return fdiv(a, b); }
+  __device__ __forceinline__ float ratio(float a, float b) { return fdiv(a, b); }
+  __device__ __forceinline__ bool unsafe() const { return false; }
+};
+
 // Adjoint of one cell in a sweep's local frame: component 1 = u1,
 // 2 = normal momentum, 3 = transverse momentum.
 struct Adj3 {
@@ -43,25 +70,25 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
                                             const FluctAdj &gf, Adj3 &ga, Adj3 &gb) {
   // ---- forward
   const float ra = q1a + 1.0f, rb = q1b + 1.0f;
-  const float vna = qna / ra, vta = qta / ra, vnb = qnb / rb, vtb = qtb / rb;
+  const float vna = fdiv(qna, ra), vta = fdiv(qta, ra), vnb = fdiv(qnb, rb), vtb = fdiv(qtb, rb);
   const float Z1 = (ra + rb) * 0.5f;
   const float Zn = (vna + vnb) * 0.5f;
   const float Zt = (vta + vtb) * 0.5f;
-  const float tmp1 = Zn / Z1;
-  const float tmp2 = (Zn * Zn) / Z1;
+  const float tmp1 = fdiv(Zn, Z1);
+  const float tmp2 = fdiv(Zn * Zn, Z1);
   const float tmp3 = tmp1 * tmp1 - 2.0f * tmp2 + 1.0f + two_bm1 * (Z1 - 1.0f);
   const float sq = sqrtf(tmp3);
   const float L1 = tmp1 + sq, L2 = tmp1 - sq, L3 = tmp1;
   const float N1 = L1 * Zt - 2.0f * Zn * Zt, D1 = L1 * Z1 - Zt;
   const float N2 = L2 * Zt - 2.0f * Zn * Zt, D2 = L2 * Z1 - Zt;
-  const float A1 = N1 / D1, A2 = N2 / D2;
+  const float A1 = fdiv(N1, D1), A2 = fdiv(N2, D2);
   const float drho = ra - rb, dun = qna - qnb;
   const float Da = L1 - L2;
-  const float a1 = (dun - drho * L2) / Da;
+  const float a1 = fdiv(dun - drho * L2, Da);
   const float a2 = drho - a1;
   const float N3 = (L1 * A2 - L2 * A1) * drho + (A1 - A2) * dun;
   const float D3 = L2 - L1;
-  const float q3 = N3 / D3;
+  const float q3 = fdiv(N3, D3);
   const float a3 = q3 + qta - qtb;
   // ---- reverse
   // fluctuations: each wave feeds amdq if its speed is negative, apdq if positive
@@ -82,8 +109,8 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
   float gA2 = m23 * L2 * a2 + gw.w32 * a2;
   // a3 = N3 / D3 + qta - qtb
   float gqta = ga3, gqtb = -ga3;
-  const float gN3 = ga3 / D3;
-  const float gD3 = -ga3 * q3 / D3;
+  const float gN3 = fdiv(ga3, D3);
+  const float gD3 = fdiv(-ga3 * q3, D3);
   gL2 += gD3;
   gL1 -= gD3;
   gL1 += gN3 * A2 * drho;
@@ -98,8 +125,8 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
   gdrho += ga2;
   ga1 -= ga2;
   // a1 = (dun - drho L2) / (L1 - L2)
-  const float gNa = ga1 / Da;
-  const float gDa = -ga1 * a1 / Da;
+  const float gNa = fdiv(ga1, Da);
+  const float gDa = fdiv(-ga1 * a1, Da);
   gdun += gNa;
   gdrho -= gNa * L2;
   gL2 -= gNa * drho;
@@ -108,14 +135,14 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
   // A1 = N1 / D1, A2 = N2 / D2
   float gZ1 = 0.f, gZn = 0.f, gZt = 0.f;
   {
-    const float gN = gA1 / D1, gD = -gA1 * A1 / D1;
+    const float gN = fdiv(gA1, D1), gD = fdiv(-gA1 * A1, D1);
     gL1 += gN * Zt + gD * Z1;
     gZt += gN * (L1 - 2.0f * Zn) - gD;
     gZn -= gN * 2.0f * Zt;
     gZ1 += gD * L1;
   }
   {
-    const float gN = gA2 / D2, gD = -gA2 * A2 / D2;
+    const float gN = fdiv(gA2, D2), gD = fdiv(-gA2 * A2, D2);
     gL2 += gN * Zt + gD * Z1;
     gZt += gN * (L2 - 2.0f * Zn) - gD;
     gZn -= gN * 2.0f * Zt;
@@ -124,13 +151,13 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
   // L1 = tmp1 + sq, L2 = tmp1 - sq, L3 = tmp1
   float gtmp1 = gL1 + gL2 + gL3;
   const float gsq = gL1 - gL2;
-  const float gtmp3 = gsq / (2.0f * sq);
+  const float gtmp3 = fdiv(gsq, 2.0f * sq);
   gtmp1 += gtmp3 * 2.0f * tmp1;
   const float gtmp2 = -2.0f * gtmp3;
   gZ1 += gtmp3 * two_bm1;
   // tmp2 = Zn^2 / Z1, tmp1 = Zn / Z1
-  gZn += gtmp2 * 2.0f * Zn / Z1 + gtmp1 / Z1;
-  gZ1 -= gtmp2 * tmp2 / Z1 + gtmp1 * tmp1 / Z1;
+  gZn += fdiv(gtmp2 * 2.0f * Zn, Z1) + fdiv(gtmp1, Z1);
+  gZ1 -= fdiv(gtmp2 * tmp2, Z1) + fdiv(gtmp1 * tmp1, Z1);
   // means
   float gra = 0.5f * gZ1, grb = 0.5f * gZ1;
   const float gvna = 0.5f * gZn, gvnb = 0.5f * gZn, gvta = 0.5f * gZt, gvtb = 0.5f * gZt;
@@ -139,12 +166,12 @@ __device__ __forceinline__ void riemann_adj(float q1a, float qna, float qta, flo
   grb -= gdrho;
   float gqna = gdun, gqnb = -gdun;
   // v = q / rho
-  gqna += gvna / ra;
-  gqta += gvta / ra;
-  gra -= (gvna * vna + gvta * vta) / ra;
-  gqnb += gvnb / rb;
-  gqtb += gvtb / rb;
-  grb -= (gvnb * vnb + gvtb * vtb) / rb;
+  gqna += fdiv(gvna, ra);
+  gqta += fdiv(gvta, ra);
+  gra -= fdiv(gvna * vna + gvta * vta, ra);
+  gqnb += fdiv(gvnb, rb);
+  gqtb += fdiv(gvtb, rb);
+  grb -= fdiv(gvnb * vnb + gvtb * vtb, rb);
   ga.q1 += gra;
   ga.qn += gqna;
   ga.qt += gqta;
@@ -187,9 +214,9 @@ __device__ __forceinline__ void correction_adj(const WaveN &wm, const WaveN &w0,
     const float dr = W0[0][p] * WP[0][p] + W0[1][p] * WP[1][p] + W0[2][p] * WP[2][p];
     const float d = up ? dl : dr;
     const bool nz = n != 0.0f;
-    const float r = nz ? d / n : 0.0f;
-    DivIEEE ieee;
-    const float phi = nz ? mc_limit(n, dl, dr, s[p], ieee) : 1.0f;
+    const float r = nz ? fdiv(d, n) : 0.0f;
+    DivFast fast;
+    const float phi = nz ? mc_limit(n, dl, dr, s[p], fast) : 1.0f;
     const float as = fabsf(s[p]);
     const float g = as * (1.0f - as * dtx);
     // f_k = 0.5 sum_p g_p W_kp phi_p
@@ -205,8 +232,8 @@ __device__ __forceinline__ void correction_adj(const WaveN &wm, const WaveN &w0,
     gs[p] += gg * (1.0f - 2.0f * as * dtx) * sgn;
     if (nz) {
       const float gr = gphi * mc_limit_dphi(r);
-      const float gd = gr / n;
-      const float gn = -gr * r / n;
+      const float gd = fdiv(gr, n);
+      const float gn = fdiv(-gr * r, n);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         g0W[k][p] += 2.0f * W0[k][p] * gn;

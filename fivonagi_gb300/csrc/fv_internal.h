@@ -83,10 +83,12 @@ __host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny
 //   chunk ids (window * chunks_per_window + chunk), one per marked chunk.
 constexpr int kFixRows = 8;
 
-// Stage kernel of the adjoint's recompute: one pass writing the
-// boundary-applied state, the state after the y sweep and after the x
-// sweep (StepArgs::stages), exact (IEEE-equal) division.
-constexpr int kStageAll = 4;
+// A full attempt (DivFma step, fix-up, finalize) that also writes the
+// boundary-applied state, the state after the y sweep and the state after
+// the x sweep (StepArgs::stages), exact in every row: the fix-up pass
+// rewrites the stage rows of the chunks it recomputes. The adjoint's
+// segment replay records its linearisation points this way.
+constexpr int kStageRecord = -2;
 __host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }
@@ -106,11 +108,11 @@ struct StepArgs {
   float *partials;        // one CFL maximum per CTA of the step launch, then
                           // one per CTA of the fix-up launch
   float *dbg[3];          // debug-stage output (stage kernels 0..3 only)
-  float *stages[9];       // kStageAll output: boundary-applied state, y-swept, x-swept
+  float *stages[9];       // kStageRecord output: boundary-applied state, y-swept, x-swept
   uint32_t *fix;          // fix-up scratch, zero between attempts (see above)
   int32_t nstrips;        // column strips of width kWarpCols * warps
   int32_t nblocks;        // CTAs of the launch
-  int64_t work;           // nstrips * ny: strip-rows to share among the CTAs
+  int64_t work;           // nstrips * ny: strip-rows (sizes the default launch)
   int32_t fix_blocks;     // CTAs of the fix-up launch
   int32_t pad0;
 };

@@ -27,9 +27,9 @@
 //    memory. A rejected step leaves the input buffer current, so the retry
 //    starts from the pre-step state.
 //
-// Work distribution: CTAs are persistent over a balanced share of the
-// (column strip, row) space, so every CTA streams the same number of rows;
-// a share may span two strips.
+// Work distribution: every warp streams a balanced share of the (window,
+// row) space, windows being the 26-column output spans, so every warp
+// streams the same number of rows; a share may span two windows.
 //
 // Division: the step kernel divides with Markstein's FMA sequence
 // (DivFma, fv_device.cuh), which equals IEEE division unless an operand is
@@ -146,7 +146,9 @@ struct FlagMarker {
 // discard the results (stores and flags are predicated), which keeps the
 // loop body free of branches.
 // EDGE: the warp's columns include ghost columns.
-// STAGE < 0: full step into `out`; STAGE 0..3: that stage's grid into `out`.
+// STAGE < 0: full step into `out`; STAGE 0..3: that stage's grid into `out`;
+// kStageRecord: the full step into out[0..2] and the stage grids B, S1, S2
+// into out[3..11].
 // DP: division policy. With DivFma, an iteration whose divisions may differ
 // from IEEE division marks the output rows it can influence (mk), and the
 // CFL and negative-eigenvalue checks that depend on it are left to the
@@ -213,11 +215,21 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   load_raw(y0 - 2, pf1);
 
   unsigned yhist = 0u;
-  const int r_end = y1 + 4;
-  for (int r = y0 - 3; r <= r_end; ++r) {
-    Cell3 u = pf0;
-    pf0 = pf1;
-    if (r + 2 <= y1 + 2) load_raw(r + 2, pf1);
+  // One iteration at loaded row r with the chains it needs: Y runs for
+  // r in [y0-3, y1+2], X for [y0+2, y1+3], D for [y0+5, y1+4]; outside
+  // those ranges a chain's results lie outside the window. The ranges are
+  // compile-time phases of the loop below, so each phase's body stays free
+  // of branches and its chains interleave.
+  auto iterate = [&](int r, auto run_y, auto run_x, auto run_d) {
+    constexpr bool RY = decltype(run_y)::value;
+    constexpr bool RX = decltype(run_x)::value;
+    constexpr bool RD = decltype(run_d)::value;
+    Cell3 u{0.f, 0.f, 0.f};
+    if constexpr (RY) {
+      u = pf0;
+      pf0 = pf1;
+      if (r + 2 <= y1 + 2) load_raw(r + 2, pf1);
+    }
 
     // ======== Y chain: interface r, flux r-1, update of row r-2
     // ======== X chain: row r-3; normal = u2, transverse = u3
@@ -270,12 +282,13 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       xo.vy2 = dp.div_r(xo.s2.u3, rr2);
     };
     DP dy, dx;
-    y_chain(dy);
-    x_chain(dx);
+    if constexpr (RY) y_chain(dy);
+    if constexpr (RX) x_chain(dx);
     bool excl_y = false, excl_x = false, flagged = false;
     if constexpr (DP::kFlags) {
-      const bool yf = __any_sync(0xffffffffu, dy.unsafe());
-      const bool xf = __any_sync(0xffffffffu, dx.unsafe());
+      bool yf = false, xf = false;
+      if constexpr (RY) yf = __any_sync(0xffffffffu, dy.unsafe());
+      if constexpr (RX) xf = __any_sync(0xffffffffu, dx.unsafe());
       yhist = (yhist << 1) | (yf ? 1u : 0u);  // bit k: y chain of iteration r-k
       excl_y = (yhist & 0x3u) != 0u;
       excl_x = xf || (yhist & 0x3eu) != 0u;
@@ -283,95 +296,105 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     }
 
     // ---- Y results
-    const float cy = (r <= 0) ? 0.0f : yo.cy;  // cfl = 0 on j == 0 (apps/na/fv.h:212-215)
-    neg = neg || (!yo.ok && !excl_y && out_lane && r >= y0 && r < y1 && r >= 1);
-    const float fn1 = ap1 + yo.f.am1, fn2 = ap2 + yo.f.am2, fn3 = ap3 + yo.f.am3;
-    const int cyr = r - 2;  // row of the y update
-    Cell3 s1 = s0_m2;
-    {
-      // local components: 1 -> u1, 2 (normal) -> u3, 3 (transverse) -> u2
-      const float m1 = s0_m2.u1 - dty * fo1;
-      const float m3 = s0_m2.u3 - dty * fo2;
-      const float m2 = s0_m2.u2 - dty * fo3;
-      const bool in_y = col_int && cyr >= 2 && cyr <= ny - 3;
-      s1.u1 = in_y ? m1 - dty * (yo.fa1 - fa1) : s0_m2.u1;
-      s1.u3 = in_y ? m3 - dty * (yo.fa2 - fa2) : s0_m2.u3;
-      s1.u2 = in_y ? m2 - dty * (yo.fa3 - fa3) : s0_m2.u2;
-    }
-    if (STAGE == FV_STAGE_BOUNDARY || STAGE == FV_STAGE_SWEEP_Y) {
-      if (out_lane && cyr >= y0 && cyr < y1) store3(out, i + cyr * nx, STAGE == FV_STAGE_BOUNDARY ? s0_m2 : s1);
-    }
-    if (STAGE == kStageAll) {
-      if (out_lane && cyr >= y0 && cyr < y1) {
-        store3(out, i + cyr * nx, s0_m2);
-        store3(out + 3, i + cyr * nx, s1);
+    if constexpr (RY) {
+      const float cy = (r <= 0) ? 0.0f : yo.cy;  // cfl = 0 on j == 0 (apps/na/fv.h:212-215)
+      neg = neg || (!yo.ok && !excl_y && out_lane && r >= y0 && r < y1 && r >= 1);
+      const float fn1 = ap1 + yo.f.am1, fn2 = ap2 + yo.f.am2, fn3 = ap3 + yo.f.am3;
+      const int cyr = r - 2;  // row of the y update
+      Cell3 s1 = s0_m2;
+      {
+        // local components: 1 -> u1, 2 (normal) -> u3, 3 (transverse) -> u2
+        const float m1 = s0_m2.u1 - dty * fo1;
+        const float m3 = s0_m2.u3 - dty * fo2;
+        const float m2 = s0_m2.u2 - dty * fo3;
+        const bool in_y = col_int && cyr >= 2 && cyr <= ny - 3;
+        s1.u1 = in_y ? m1 - dty * (yo.fa1 - fa1) : s0_m2.u1;
+        s1.u3 = in_y ? m3 - dty * (yo.fa2 - fa2) : s0_m2.u3;
+        s1.u2 = in_y ? m2 - dty * (yo.fa3 - fa3) : s0_m2.u2;
       }
+      if (STAGE == FV_STAGE_BOUNDARY || STAGE == FV_STAGE_SWEEP_Y) {
+        if (out_lane && cyr >= y0 && cyr < y1) store3(out, i + cyr * nx, STAGE == FV_STAGE_BOUNDARY ? s0_m2 : s1);
+      }
+      if (STAGE == kStageRecord) {
+        if (out_lane && cyr >= y0 && cyr < y1) {
+          store3(out + 3, i + cyr * nx, s0_m2);
+          store3(out + 6, i + cyr * nx, s1);
+        }
+      }
+      // rotate the Y chain's carried values (the X chain of this iteration
+      // has already read s1_m3 and cy_m3)
+      s0_m2 = s0_m1;
+      s0_m1 = u;
+      vx_m1 = yo.vx;
+      vy_m1 = yo.vy;
+      w_m1 = yo.w;
+      dl_m1 = yo.dr;
+      ap1 = yo.f.ap1; ap2 = yo.f.ap2; ap3 = yo.f.ap3;
+      fo1 = fn1; fo2 = fn2; fo3 = fn3;
+      fa1 = yo.fa1; fa2 = yo.fa2; fa3 = yo.fa3;
+      cy_m3 = cy_m2;
+      cy_m2 = cy_m1;
+      cy_m1 = cy;
+      s1_m3 = s1;
     }
 
     // ---- X results
-    const int cxr = r - 3;
-    const bool own_x = out_lane && cxr >= y0 && cxr < y1;
-    neg = neg || (!xo.ok && !excl_x && own_x && i >= 1);
-    {
-      // CFL of cell (i, r-3): its y and x interfaces; 0 on i == 0
-      const float cell = (i == 0) ? 0.0f : xo.cx;
-      const bool counted = own_x && !excl_x && (!even_only || ((i + cxr * nx) & 1) == 0);
-      cmax = counted ? nanmax(cmax, cell) : cmax;
-    }
-    if (STAGE == FV_STAGE_SWEEP_X) {
-      if (own_x) store3(out, i + cxr * nx, xo.s2);
-    }
-    if (STAGE == kStageAll) {
-      if (own_x) store3(out + 6, i + cxr * nx, xo.s2);
+    if constexpr (RX) {
+      const int cxr = r - 3;
+      const bool own_x = out_lane && cxr >= y0 && cxr < y1;
+      neg = neg || (!xo.ok && !excl_x && own_x && i >= 1);
+      {
+        // CFL of cell (i, r-3): its y and x interfaces; 0 on i == 0
+        const float cell = (i == 0) ? 0.0f : xo.cx;
+        const bool counted = own_x && !excl_x && (!even_only || ((i + cxr * nx) & 1) == 0);
+        cmax = counted ? nanmax(cmax, cell) : cmax;
+      }
+      if (STAGE == FV_STAGE_SWEEP_X) {
+        if (own_x) store3(out, i + cxr * nx, xo.s2);
+      }
+      if (STAGE == kStageRecord) {
+        if (own_x) store3(out + 9, i + cxr * nx, xo.s2);
+      }
     }
 
     // ======== D chain: diffusion of row r-5 (apps/na/source.h:22-104)
-    const int cdr = r - 5;
-    const float vxl = shup(vx2_m5), vyl = shup(vy2_m5);
-    const float vxr = shdn(vx2_m5), vyr = shdn(vy2_m5);
-    if (STAGE < 0 || STAGE == FV_STAGE_SOURCE) {
-      const bool in_d = col_int && cdr >= 2 && cdr <= ny - 3;
-      Cell3 o3;
-      o3.u1 = in_d ? (s2_m5.u1 + 1.0f) - 1.0f : s2_m5.u1;
-      o3.u2 = in_d ? s2_m5.u2 + ddtx2 * (vxl - 2.0f * vx2_m5 + vxr) +
-                         ddty2 * (vx2_m6 - 2.0f * vx2_m5 + vx2_m4)
-                   : s2_m5.u2;
-      o3.u3 = in_d ? s2_m5.u3 + ddtx2 * (vyl - 2.0f * vy2_m5 + vyr) +
-                         ddty2 * (vy2_m6 - 2.0f * vy2_m5 + vy2_m4)
-                   : s2_m5.u3;
-      if (out_lane && cdr >= y0 && cdr < y1) {
-        if (STAGE < 0) {
-          // moving window (moveDomain, common/main.cu:109-164): the new
-          // cell (i - shx, j - shy) takes this cell's value, and a cell
-          // whose source would lie past the far edge keeps its own value
-          const int ti = i - shx, tj = cdr - shy;
-          if (ti >= 0 && tj >= 0) store3(out, ti + tj * nx, o3);
-          if (i + shx > nx - 1 || cdr + shy > ny - 1) store3(out, i + cdr * nx, o3);
-        } else {
-          store3(out, i + cdr * nx, o3);
+    if constexpr (RD) {
+      const int cdr = r - 5;
+      const float vxl = shup(vx2_m5), vyl = shup(vy2_m5);
+      const float vxr = shdn(vx2_m5), vyr = shdn(vy2_m5);
+      if (STAGE < 0 || STAGE == FV_STAGE_SOURCE) {
+        const bool in_d = col_int && cdr >= 2 && cdr <= ny - 3;
+        Cell3 o3;
+        o3.u1 = in_d ? (s2_m5.u1 + 1.0f) - 1.0f : s2_m5.u1;
+        o3.u2 = in_d ? s2_m5.u2 + ddtx2 * (vxl - 2.0f * vx2_m5 + vxr) +
+                           ddty2 * (vx2_m6 - 2.0f * vx2_m5 + vx2_m4)
+                     : s2_m5.u2;
+        o3.u3 = in_d ? s2_m5.u3 + ddtx2 * (vyl - 2.0f * vy2_m5 + vyr) +
+                           ddty2 * (vy2_m6 - 2.0f * vy2_m5 + vy2_m4)
+                     : s2_m5.u3;
+        if (out_lane && cdr >= y0 && cdr < y1) {
+          if (STAGE < 0) {
+            // moving window (moveDomain, common/main.cu:109-164): the new
+            // cell (i - shx, j - shy) takes this cell's value, and a cell
+            // whose source would lie past the far edge keeps its own value
+            const int ti = i - shx, tj = cdr - shy;
+            if (ti >= 0 && tj >= 0) store3(out, ti + tj * nx, o3);
+            if (i + shx > nx - 1 || cdr + shy > ny - 1) store3(out, i + cdr * nx, o3);
+          } else {
+            store3(out, i + cdr * nx, o3);
+          }
         }
       }
     }
 
-    // ======== rotate
-    s0_m2 = s0_m1;
-    s0_m1 = u;
-    vx_m1 = yo.vx;
-    vy_m1 = yo.vy;
-    w_m1 = yo.w;
-    dl_m1 = yo.dr;
-    ap1 = yo.f.ap1; ap2 = yo.f.ap2; ap3 = yo.f.ap3;
-    fo1 = fn1; fo2 = fn2; fo3 = fn3;
-    fa1 = yo.fa1; fa2 = yo.fa2; fa3 = yo.fa3;
-    cy_m3 = cy_m2;
-    cy_m2 = cy_m1;
-    cy_m1 = cy;
-    s1_m3 = s1;
-    s2_m5 = s2_m4;
-    s2_m4 = xo.s2;
-    vx2_m6 = vx2_m5; vy2_m6 = vy2_m5;
-    vx2_m5 = vx2_m4; vy2_m5 = vy2_m4;
-    vx2_m4 = xo.vx2; vy2_m4 = xo.vy2;
+    // ======== rotate the X chain's results (read by the D chain above)
+    if constexpr (RX) {
+      s2_m5 = s2_m4;
+      s2_m4 = xo.s2;
+      vx2_m6 = vx2_m5; vy2_m6 = vy2_m5;
+      vx2_m5 = vx2_m4; vy2_m5 = vy2_m4;
+      vx2_m4 = xo.vx2; vy2_m4 = xo.vy2;
+    }
 
     // ======== rare: mark the rows this iteration can influence
     if constexpr (DP::kFlags) {
@@ -380,7 +403,15 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
         if (lo <= hi) mk.mark(xw, lo, hi);
       }
     }
-  }
+  };
+  const std::true_type on{};
+  const std::false_type off{};
+  int r = y0 - 3;
+  for (; r <= y0 + 1; ++r) iterate(r, on, off, off);  // warm-up: Y only
+  for (const int e = min(y0 + 4, y1 + 2); r <= e; ++r) iterate(r, on, on, off);
+  for (; r <= y1 + 2; ++r) iterate(r, on, on, on);
+  iterate(y1 + 3, off, on, on);  // drain
+  iterate(y1 + 4, off, off, on);
 }
 
 // Accept or reject an attempt from its CFL, and update dt/T/n/cur/MDX/MDY
@@ -511,9 +542,9 @@ __device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg,
 }
 
 // The step: STAGE < 0 is the full attempt with FMA division, followed by
-// the fix-up and finalize launches; STAGE 0..3 write that stage's grid to
-// the debug buffers with IEEE division; kStageAll writes the first three
-// stages' grids at once (the adjoint's recompute).
+// the fix-up and finalize launches (kStageRecord also writes the stage
+// grids); STAGE 0..3 write that stage's grid to the debug buffers with IEEE
+// division.
 template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   __shared__ float red[kWarps];
@@ -528,9 +559,10 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   int shx = 0, shy = 0;
   if (STAGE < 0) window_shift(a.p, T, dt, mdx, mdy, shx, shy);
   const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
-  float *out[STAGE == kStageAll ? 9 : 3];
-  if constexpr (STAGE == kStageAll) {
-    for (int k = 0; k < 9; ++k) out[k] = a.stages[k];
+  float *out[STAGE == kStageRecord ? 12 : 3];
+  if constexpr (STAGE == kStageRecord) {
+    for (int f = 0; f < 3; ++f) out[f] = a.state[cur ^ 1][f];
+    for (int k = 0; k < 9; ++k) out[3 + k] = a.stages[k];
   } else {
     for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
   }
@@ -541,32 +573,26 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   const int ny = a.p.ny;
   float cmax = 0.0f;
   bool neg = false;
-  const long long W = a.work;
-  const long long b = blockIdx.x;
-  const long long s0 = b * W / a.nblocks, s1 = (b + 1) * W / a.nblocks;
+  // Each warp streams a balanced share of the (window, row) pairs, windows
+  // of kWarpCols output columns: every warp of the launch gets the same
+  // number of rows, whatever the last window's width.
+  const long long windows = (a.p.nx + kWarpCols - 1) / kWarpCols;
+  const long long W = windows * ny;
+  const long long G = (long long)a.nblocks * kWarps;
+  const long long g = (long long)blockIdx.x * kWarps + warp;
+  const long long s0 = g * W / G, s1 = (g + 1) * W / G;
   for (long long pos = s0; pos < s1;) {
-    const int strip = (int)(pos / ny);
-    const int y0 = (int)(pos - (long long)strip * ny);
+    const int win = (int)(pos / ny);
+    const int y0 = (int)(pos - (long long)win * ny);
     const long long left = s1 - pos;
     const int y1 = (int)((long long)y0 + left < ny ? (long long)y0 + left : ny);
-    const int xw = strip * kStripCols + warp * kWarpCols;
-    if (xw < a.p.nx) {
-      if constexpr (STAGE < 0) {
-        StepMarker mk{a, -1};
-        stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
-      } else if constexpr (STAGE == kStageAll) {
-        // exact division without branches; a warp whose operands leave
-        // DivExact's range redoes its segment with IEEE division
-        FlagMarker fm;
-        stream_window<STAGE, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, fm);
-        if (__any_sync(0xffffffffu, fm.flagged)) {
-          NoMarker mk;
-          stream_window<STAGE, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
-        }
-      } else {
-        NoMarker mk;
-        stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
-      }
+    const int xw = win * kWarpCols;
+    if constexpr (STAGE < 0) {
+      StepMarker mk{a, -1};
+      stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+    } else {
+      NoMarker mk;
+      stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
     }
     pos += y1 - y0;
   }
@@ -585,6 +611,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
 constexpr int kFixItemRows = 2;
 static_assert(kFixRows % kFixItemRows == 0, "fix-up items must tile a chunk");
 
+// STAGE: -1, or kStageRecord (the chunks' stage rows are rewritten too).
+template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
   __shared__ float red[kWarps];
   __shared__ int sh[1];
@@ -597,7 +625,11 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
   int shx = 0, shy = 0;
   window_shift(a.p, T, dt, mdx, mdy, shx, shy);
   const float *in[3] = {a.state[cur][0], a.state[cur][1], a.state[cur][2]};
-  float *out[3] = {a.state[cur ^ 1][0], a.state[cur ^ 1][1], a.state[cur ^ 1][2]};
+  float *out[STAGE == kStageRecord ? 12 : 3];
+  for (int f = 0; f < 3; ++f) out[f] = a.state[cur ^ 1][f];
+  if constexpr (STAGE == kStageRecord) {
+    for (int k = 0; k < 9; ++k) out[3 + k] = a.stages[k];
+  }
   const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
   const int lane = threadIdx.x & 31;
   const int ny = a.p.ny;
@@ -617,19 +649,19 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
     const unsigned id = __ldcg(list + k / kItems);
     const int window = (int)(id / (unsigned)cpw), c = (int)(id - (unsigned)window * (unsigned)cpw);
     if (lane == 0 && k % kItems == 0u) atomicAnd(a.fix + 4 + (id >> 5), ~(1u << (id & 31u)));
-    const int xw = window * kWarpCols;  // strip * kStripCols + warp * kWarpCols
+    const int xw = window * kWarpCols;
     const int y0 = c * kFixRows + (int)(k % kItems) * kFixItemRows;
     if (y0 >= ny) continue;
     const int y1 = min(ny, y0 + kFixItemRows);
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<-1, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    stream_window<STAGE, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
       NoMarker none;
-      stream_window<-1, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+      stream_window<STAGE, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
     }
     cmax = nanmax(cmax, cm);
     neg = neg || ng;
@@ -909,14 +941,18 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
   switch (stage) {
     case -1:
       step_kernel<-1><<<grid, block, 0, st>>>(a);
-      fixup_kernel<<<a.fix_blocks, block, 0, st>>>(a);
+      fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);
+      finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
+      break;
+    case kStageRecord:
+      step_kernel<kStageRecord><<<grid, block, 0, st>>>(a);
+      fixup_kernel<kStageRecord><<<a.fix_blocks, block, 0, st>>>(a);
       finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;
     case 0: step_kernel<0><<<grid, block, 0, st>>>(a); break;
     case 1: step_kernel<1><<<grid, block, 0, st>>>(a); break;
     case 2: step_kernel<2><<<grid, block, 0, st>>>(a); break;
     case 3: step_kernel<3><<<grid, block, 0, st>>>(a); break;
-    case kStageAll: step_kernel<kStageAll><<<grid, block, 0, st>>>(a); break;
     default: return (int)cudaErrorInvalidValue;
   }
   return (int)cudaGetLastError();

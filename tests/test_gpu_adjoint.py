@@ -121,3 +121,21 @@ def test_replays_repeat_and_backward_needs_a_new_forward():
     adj.forward(amp, ph)
     adj.backward()
     adj.close()
+
+
+def test_backward_repeats_and_keeps_the_final_state():
+    """An odd step count leaves the final state in the second buffer; the
+    backward's segment replays must not lose track of it."""
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 5, p.ampl)
+    n = NSTEPS - 1
+    adj = Adjoint(p, loss_window(14, 18, 8, 8, 60, n), n, checkpoint_every=10)
+    adj.forward(amp, ph)
+    before = adj.get_state()
+    ga1, gp1 = adj.backward()
+    after = adj.get_state()
+    ga2, gp2 = adj.backward()
+    for f in range(3):
+        assert same_values(before[f], after[f])
+    assert np.array_equal(ga1, ga2) and np.array_equal(gp1, gp2)
+    adj.close()
