@@ -519,8 +519,9 @@ def run_adjoint(args):
     from fivonagi_gb300 import _abi
 
     p = _abi.default_params("phased-array")
-    nsteps = 4000
-    _time_design(p, *_adjoint_case(p, (700, 512), 200, args.seed), 200)  # warm-up: first launches
+    nsteps = args.adjoint_steps or 4000
+    warm = min(200, nsteps)
+    _time_design(p, *_adjoint_case(p, (700, 512), warm, args.seed), warm)  # warm-up: first launches
     amp, ph, win = _adjoint_case(p, (700, 512), nsteps, args.seed)
     r = _time_design(p, amp, ph, win, nsteps, fd_params=2)
     cells = p.nx * p.ny
@@ -533,14 +534,15 @@ def run_adjoint(args):
         "unit": "ratio",
         "n_gpus": 1,
         "steps": nsteps,
-        "warmup": 200,
+        "warmup": warm,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "phased array 1024x1024, 128 elements x (amplitude, phase), loss window 32x32 "
-                               "at (700, 512) over steps 3501-4000, checkpoint every ceil(sqrt(N)) steps",
+                               f"at (700, 512) over steps {max(1, nsteps - 499)}-{nsteps}, checkpoint every "
+                               "ceil(sqrt(N)) steps",
                    "seed": args.seed},
         "forward_plain_s": r["t_plain"],
         "forward_recorded_s": r["t_fwd"],
@@ -567,14 +569,15 @@ def run_designs(args):
 
     base = _abi.default_params("phased-array")
     p = base.replace(nx=2048, ny=1024, xmax=2047 / 24, ymax=1023 / 24, center=512.0)
-    nsteps = 6000
+    nsteps = args.adjoint_steps or 6000
+    warm = min(200, nsteps)
     rng = np.random.default_rng(args.seed)
     targets = [(1024 + 128 * (k % 8) + 64, 128 * (k // 8) + 64) for k in rng.permutation(64)]
     results = []
     t_all = 0.0
     for d in range(args.designs):
         if d == 0:
-            _time_design(p, *_adjoint_case(p, targets[d], 200, args.seed), 200)  # warm-up
+            _time_design(p, *_adjoint_case(p, targets[d], warm, args.seed), warm)  # warm-up
         amp, ph, win = _adjoint_case(p, targets[d], nsteps, args.seed + 1000 + d)
         r = _time_design(p, amp, ph, win, nsteps, fd_params=1 if d == 0 else 0)
         t_all += r["t_fwd"] + r["t_bwd"]
@@ -585,13 +588,13 @@ def run_designs(args):
         "unit": "gradients/s",
         "n_gpus": 1,
         "steps": nsteps,
-        "warmup": 200,
+        "warmup": warm,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{len(results)} phased-array designs 2048x1024, 6000 steps, 256 weights each, "
+        "config": {"workload": f"{len(results)} phased-array designs 2048x1024, {nsteps} steps, 256 weights each, "
                                "32x32 focal windows from an 8x8 grid in the right half", "seed": args.seed},
         "adjoint_forward_ratio_mean": float(np.mean([r["t_bwd"] / r["t_plain"] for r in results])),
         "adjoint_memory_gb_max": max(r["mem"] for r in results) / 1e9,
@@ -616,6 +619,9 @@ def main():
                          "adjoint: config-4 gradient; designs: config-5 gradients")
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--designs", type=int, default=32)
+    ap.add_argument("--adjoint-steps", type=int, default=0,
+                    help="adjoint and designs workloads: steps instead of the configuration's (a small "
+                         "case for a profiler's launch list)")
     ap.add_argument("--blocks", type=int, default=0,
                     help="plain workload: CTAs per step launch instead of the autotuner's choice")
     ap.add_argument("--seed", type=int, default=0)

@@ -142,9 +142,9 @@ struct FlagMarker {
 //   X: x sweep of row r-3 (S1 of the previous iteration -> S2) and the CFL
 //      of its cells;
 //   D: diffusion of row r-5 from S2 of rows r-6, r-5, r-4 (source).
-// Warm-up and drain iterations compute on rows outside [y0-1, y1] and
-// discard the results (stores and flags are predicated), which keeps the
-// loop body free of branches.
+// Warm-up and drain iterations run only the chains whose results the
+// window needs (three phases, below); results on rows outside the window
+// are discarded (stores and checks are predicated).
 // EDGE: the warp's columns include ghost columns.
 // STAGE < 0: full step into `out`; STAGE 0..3: that stage's grid into `out`;
 // kStageRecord: the full step into out[0..2] and the stage grids B, S1, S2
@@ -215,11 +215,14 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   load_raw(y0 - 2, pf1);
 
   unsigned yhist = 0u;
-  // One iteration at loaded row r with the chains it needs: Y runs for
-  // r in [y0-3, y1+2], X for [y0+2, y1+3], D for [y0+5, y1+4]; outside
-  // those ranges a chain's results lie outside the window. The ranges are
-  // compile-time phases of the loop below, so each phase's body stays free
-  // of branches and its chains interleave.
+  // One iteration at loaded row r with the chains it needs. Y's results
+  // are used for r in [y0-3, y1+2], X's for [y0+2, y1+3], D's for
+  // [y0+5, y1+4]. The loop below runs three compile-time phases: Y alone
+  // for r <= y0+1, all three chains up to y1+2, X and D for the last two
+  // (the other chains' results there lie outside the window, and their
+  // stores and checks are predicated on the window's rows). Each phase's
+  // body stays free of branches, so its chains interleave; three copies
+  // of the body keep the instruction footprint small.
   auto iterate = [&](int r, auto run_y, auto run_x, auto run_d) {
     constexpr bool RY = decltype(run_y)::value;
     constexpr bool RX = decltype(run_x)::value;
@@ -408,10 +411,8 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   const std::false_type off{};
   int r = y0 - 3;
   for (; r <= y0 + 1; ++r) iterate(r, on, off, off);  // warm-up: Y only
-  for (const int e = min(y0 + 4, y1 + 2); r <= e; ++r) iterate(r, on, on, off);
   for (; r <= y1 + 2; ++r) iterate(r, on, on, on);
-  iterate(y1 + 3, off, on, on);  // drain
-  iterate(y1 + 4, off, off, on);
+  for (; r <= y1 + 4; ++r) iterate(r, off, on, on);  // drain: no Y
 }
 
 // Accept or reject an attempt from its CFL, and update dt/T/n/cur/MDX/MDY
