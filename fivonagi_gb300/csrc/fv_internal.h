@@ -78,7 +78,7 @@ __host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny
 // division; a second kernel recomputes those rows with exact division. Rows
 // are marked in chunks of kFixRows rows of one warp window (the 26 output
 // columns of one warp of a strip). Layout of the uint32 scratch:
-//   [0] number of listed chunks   [1] fix-up work cursor   [2], [3] unused
+//   [0] number of listed chunks   [1], [2], [3] unused
 //   bitmap of marked chunks (one bit per chunk), then the list of marked
 //   chunk ids (window * chunks_per_window + chunk), one per marked chunk.
 constexpr int kFixRows = 8;

@@ -161,7 +161,9 @@ struct FlagMarker {
 //   marks rows f-4 .. f+3. The CFL of row r-3, taken in iteration r,
 //   depends on y chains r-5 .. r-1 and the x chain r; the y solve's
 //   eigenvalue check at interface r on y chains r-1 and r.
-template <int STAGE, bool EDGE, class DP, class MK>
+// PRE: rows loaded ahead of the one in use (the fix-up's short items load
+// all their rows at once).
+template <int STAGE, bool EDGE, class DP, int PRE, class MK>
 __device__ __forceinline__ void stream_strip(const DevParams &p, const float *const *in,
                                              const float *const *frame,
                                              float *const *out, int xw, int y0, int y1,
@@ -210,9 +212,10 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       v = Cell3{0.f, 0.f, 0.f};
     }
   };
-  Cell3 pf0, pf1;  // prefetched raw rows r, r+1
-  load_raw(y0 - 3, pf0);
-  load_raw(y0 - 2, pf1);
+  static_assert(PRE >= 1, "at least the row in use");
+  Cell3 pf[PRE];  // prefetched raw rows r .. r+PRE-1
+#pragma unroll
+  for (int k = 0; k < PRE; ++k) load_raw(y0 - 3 + k, pf[k]);
 
   unsigned yhist = 0u;
   // One iteration at loaded row r with the chains it needs. Y's results
@@ -229,9 +232,10 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     constexpr bool RD = decltype(run_d)::value;
     Cell3 u{0.f, 0.f, 0.f};
     if constexpr (RY) {
-      u = pf0;
-      pf0 = pf1;
-      if (r + 2 <= y1 + 2) load_raw(r + 2, pf1);
+      u = pf[0];
+#pragma unroll
+      for (int k = 0; k + 1 < PRE; ++k) pf[k] = pf[k + 1];
+      if (r + PRE <= y1 + 2) load_raw(r + PRE, pf[PRE - 1]);
     }
 
     // ======== Y chain: interface r, flux r-1, update of row r-2
@@ -508,8 +512,9 @@ __device__ __forceinline__ void window_shift(const DevParams &p, float T, float 
   }
 }
 
-// One warp's window [y0, y1) at column xw, with the division policy DP.
-template <int STAGE, class DP, class MK>
+// One warp's window [y0, y1) at column xw, with the division policy DP and
+// PRE rows loaded ahead.
+template <int STAGE, class DP, int PRE = 2, class MK>
 __device__ __forceinline__ void stream_window(const DevParams &p, const float *const *in,
                                               const float *const *frame, float *const *out,
                                               int xw, int y0, int y1, float dt, float T, int mdx,
@@ -518,9 +523,9 @@ __device__ __forceinline__ void stream_window(const DevParams &p, const float *c
   // ghost columns among the warp's 32 columns?
   const bool edge = (xw - kHalo <= 1) || (xw + kLanes - kHalo - 1 >= p.nx - 2);
   if (edge)
-    stream_strip<STAGE, true, DP>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+    stream_strip<STAGE, true, DP, PRE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
   else
-    stream_strip<STAGE, false, DP>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+    stream_strip<STAGE, false, DP, PRE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
 }
 
 // The CTA's CFL maximum into partials[slot], and the negative-eigenvalue
@@ -603,18 +608,21 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
 
 // Recomputes the chunks the step launch marked, with exact division
 // (DivExact), before finalize_kernel decides the attempt. Each chunk is split
-// into items of kFixItemRows rows; warps take items from a shared cursor.
-// The rows of an item are a serial loop (plus the pipeline's 8 rows of
-// warm-up and drain) that runs with few other warps on its SM, so its
-// latency, not the work, sets the pass's duration: short items keep it
-// small. An item whose operands fall outside DivExact's range (never in a
-// physical state) is redone with IEEE division.
+// into items of kFixItemRows rows; warp w of the launch takes items w,
+// w + W, w + 2W, ... (W warps). The rows of an item are a serial loop
+// (plus the pipeline's warm-up and drain) that runs with few other warps on
+// its SM, so its latency, not the work, sets the pass's duration: short
+// items, no shared cursor, and all of an item's input rows loaded at once
+// (kFixPrefetch) keep it small. An item whose operands fall outside
+// DivExact's range (never in a physical state) is redone with IEEE
+// division.
 constexpr int kFixItemRows = 2;
+constexpr int kFixPrefetch = kFixItemRows + 6;  // input rows y0-3 .. y1+2 of an item
 static_assert(kFixRows % kFixItemRows == 0, "fix-up items must tile a chunk");
 
 // STAGE: -1, or kStageRecord (the chunks' stage rows are rewritten too).
 template <int STAGE>
-__global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) fixup_kernel(StepArgs a) {
   __shared__ float red[kWarps];
   __shared__ int sh[1];
   const Ctrl *ctl = a.ctrl;
@@ -642,11 +650,8 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
   if (n == 0u) return;  // nothing marked: the finalize launch reads the step's partials only
   float cmax = 0.0f;
   bool neg = false;
-  for (;;) {
-    unsigned k = n;
-    if (lane == 0) k = atomicAdd(a.fix + 1, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= n) break;
+  const unsigned nw = gridDim.x * kWarps;
+  for (unsigned k = blockIdx.x * kWarps + (threadIdx.x >> 5); k < n; k += nw) {
     const unsigned id = __ldcg(list + k / kItems);
     const int window = (int)(id / (unsigned)cpw), c = (int)(id - (unsigned)window * (unsigned)cpw);
     if (lane == 0 && k % kItems == 0u) atomicAnd(a.fix + 4 + (id >> 5), ~(1u << (id & 31u)));
@@ -657,7 +662,8 @@ __global__ void __launch_bounds__(kThreads, 4) fixup_kernel(StepArgs a) {
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<STAGE, DivExact>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    stream_window<STAGE, DivExact, kFixPrefetch>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm,
+                                                 ng, fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
@@ -842,18 +848,15 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
 // simulation in items of kFixItemRows rows with exact division (as
 // fixup_kernel) and folds their CFL and eigenvalue checks into the
 // simulation's atomics; batch_finalize_kernel then decides.
-__global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, 2) batch_fixup_kernel(BatchArgs b) {
   const int lane = threadIdx.x & 31;
   constexpr unsigned kItems = kFixRows / kFixItemRows;
   const long long words = (b.fix_chunks + 31) / 32;
   const uint32_t *list = b.fix + 4 + words;
   const unsigned n = __ldcg(b.fix) * kItems;
   if (n == 0u) return;
-  for (;;) {
-    unsigned k = n;
-    if (lane == 0) k = atomicAdd(b.fix + 1, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= n) break;
+  const unsigned nw = gridDim.x * kWarps;
+  for (unsigned k = blockIdx.x * kWarps + (threadIdx.x >> 5); k < n; k += nw) {
     const unsigned e = k / kItems;
     const unsigned id = __ldcg(list + 2 * (long long)e);
     const int inst = (int)__ldcg(list + 2 * (long long)e + 1);
@@ -880,7 +883,7 @@ __global__ void __launch_bounds__(kThreads, 4) batch_fixup_kernel(BatchArgs b) {
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<-1, DivExact>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    stream_window<-1, DivExact, kFixPrefetch>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
