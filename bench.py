@@ -18,7 +18,9 @@ y and x sweeps, CFL reduction and dt control, diffusion).
           region.
   roofline : the step kernel against the measured HBM copy bandwidth, with
           24 algorithmic bytes per cell-update (3 FP32 fields read once and
-          written once).
+          written once) over the step kernel's own duration (CUDA events
+          between an attempt's launches); `issue` carries the kernel's
+          issue-slot figures from the committed ncu summary.
   cpu_baseline : the oracle's CPU restatement (FP32, OpenMP over rows, all
           host cores) on a bounded sample of the same grid.
 
@@ -131,11 +133,12 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
+def profiled_figures():
+    """DRAM bytes per launch and issue figures of the step kernel from the
+    committed ncu summary (profiles/), or None."""
     try:
         with open(PROFILE_TRAFFIC) as f:
-            d = json.load(f)
-        return d.get("bytes_per_launch")
+            return json.load(f)
     except (OSError, ValueError):
         return None
 
@@ -270,6 +273,11 @@ def run_gpu(args):
     sim.sync()
     del flush
     flushed_ms = statistics.median(flushed)
+
+    # ---- the step kernel alone: attempts launched one at a time with CUDA
+    # events on the solver's stream between their launches (the inputs are
+    # the 201 MB state, larger than L2)
+    step_kernel_ms, attempt_unfused_ms = sim.time_attempts(min(200, max(1, args.steps)))
     sim.close()
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -309,20 +317,28 @@ def run_gpu(args):
 
     peak, peak_kind = measured_peak()
     alg_bytes = ALG_BYTES_PER_CELL * cells
-    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
-    traffic = profiled_traffic()
+    achieved = alg_bytes / (step_kernel_ms * 1e-3) / 1e9
+    prof = profiled_figures() or {}
     roofline = {
         "bound": "hbm",
         "achieved": achieved,
         "peak": peak,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "peak_source": f"hbm_gbs, {peak_kind} (MEASURED_PEAKS.json)",
-        "traffic": traffic,
+        "peak_source": f"hbm_gbs, {peak_kind} (MEASURED_PEAKS.json); of measured",
+        "traffic": prof.get("bytes_per_launch"),
         "kernel": "step_kernel (fused y/x sweeps, CFL, diffusion)",
         "bytes_per_launch": alg_bytes,
-        "launch_ms": per_launch_ms,
-        "launch_ms_l2_flushed": flushed_ms,
+        "launch_ms": step_kernel_ms,
+        "launch_timing": "step kernel alone, CUDA events between an attempt's launches on the solver's stream",
+        "attempt_ms": per_launch_ms,
+        "attempt_ms_unfused": attempt_unfused_ms,
+        "attempt_ms_l2_flushed": flushed_ms,
+        "issue": {"bound": "instruction issue (the bound that applies to this kernel)",
+                  "ipc": prof.get("ipc_active"), "ipc_peak": prof.get("ipc_peak"),
+                  "issue_slots_busy": prof.get("issue_slots_busy"),
+                  "warp_instructions_per_launch": prof.get("warp_instructions_per_launch"),
+                  "source": "ncu --set full, profiles/step_kernel_focused_beam_4096x2048.md"},
     }
 
     line = {
@@ -345,7 +361,7 @@ def run_gpu(args):
             "cfl_target": params.cflwhish, "accepted": accepted, "rejected": int(st["rejected"]),
             "T_end": st["T"],
             "l2": "inputs larger than L2: each step reads one 100.7 MB state buffer and writes the "
-                  "other, 201 MB per step > 129 MB L2; launch_ms_l2_flushed is one step after "
+                  "other, 201 MB per step > 129 MB L2; attempt_ms_l2_flushed is one step after "
                   "writing 258 MB",
             "parallelism": "replicas" if world > 1 else "single GPU",
             "ctas_per_launch": blocks,

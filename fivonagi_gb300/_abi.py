@@ -209,6 +209,7 @@ PROTOTYPES = {
     "fv_run": (C.c_int, [_P, C.c_int64, C.POINTER(FvRunStats)]),
     "fv_run_until": (C.c_int, [_P, C.c_double, C.POINTER(FvRunStats)]),
     "fv_launch_attempts": (C.c_int, [_P, C.c_int64]),
+    "fv_time_attempts": (C.c_int, [_P, C.c_int32, _P, _P]),
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "fv_set_launch": (C.c_int, [_P, C.c_int32]),

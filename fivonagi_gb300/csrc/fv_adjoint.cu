@@ -374,25 +374,31 @@ __global__ void adj_boundary_kernel(DevParams p, CG3 lb, G3 lp) {
 
 // Weight gradients of one step from the adjoints of the source ghost cells:
 // u1 = pack, u2 = pack (pack + 1), pack = amp ramp(T) sin(ISPW T + phase).
+// One warp per element: the lanes load the element's ghost cells at once
+// (a strided loop when an element spans more than 16 rows), a warp
+// reduction in FP64 sums them, and lane 0 updates the element's sums.
 __global__ void adj_weights_kernel(DevParams p, float T, CG3 lb, double *g_amp, double *g_ph) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= p.nelem) return;
+  const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (e >= p.nelem) return;  // warp-uniform
   const float amp = p.weights[e], ph = p.weights[p.nelem + e];
   const float ramp = gmin(gmax(T * p.ramp, 0.0f), 1.0f);
   const float arg = p.ispw * T + ph;
-  const float sn = fvm::sinf_(arg), cs = fvm::cosf_(arg);
+  const float sn = fvm::sinf_(arg);
   const float pack = amp * ramp * sn;
   double sum = 0.0;
-  for (int r = 0; r < p.arr_elem; ++r) {
-    const int j = p.arr_j0 + e * p.arr_elem + r;
+  for (int k = lane; k < 2 * p.arr_elem; k += 32) {
+    const int j = p.arr_j0 + e * p.arr_elem + (k >> 1), i = k & 1;
     if (j < 2 || j > p.ny - 3) continue;  // corners are zero, not the source
-    for (int i = 0; i < 2; ++i) {
-      const size_t q = size_t(i) + size_t(j) * p.nx;
-      sum += (double)lb.f[0][q] + (double)lb.f[1][q] * (2.0 * pack + 1.0);
-    }
+    const size_t q = size_t(i) + size_t(j) * p.nx;
+    sum += (double)lb.f[0][q] + (double)lb.f[1][q] * (2.0 * pack + 1.0);
   }
-  g_amp[e] += sum * (double)ramp * (double)sn;
-  g_ph[e] += sum * (double)amp * (double)ramp * (double)cs;
+  for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+  if (lane == 0) {
+    const float cs = fvm::cosf_(arg);
+    g_amp[e] += sum * (double)ramp * (double)sn;
+    g_ph[e] += sum * (double)amp * (double)ramp * (double)cs;
+  }
 }
 
 // Loss gradient of the state after accepted step n: 2 u1 coef on the window.
@@ -637,7 +643,7 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   const long long work = (long long)a->nstrips * p->ny;
   const int per_sm = a->exact ? max_blocks_per_sm_exact(kWarpsPerStep, -1) : max_blocks_per_sm_fast(kWarpsPerStep, -1);
   a->max_resident = per_sm * a->sms;
-  a->nblocks = int(std::max(1LL, std::min(4LL * a->max_resident, work / 32)));
+  a->nblocks = int(std::max(1LL, std::min((long long)a->max_resident, work / 32)));  // one wave
   a->fix_blocks = 4 * a->sms;
   a->fix_words = size_t(fix_scratch_words((long long)a->nstrips * kWarpsPerStep, p->ny));
   e = cudaMalloc(&a->frame, 3 * size_t(frame_cells(p->nx, p->ny)) * sizeof(float));
@@ -792,7 +798,7 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
       adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(stage[0]), cg3(a->tmp[1]), ws, as);
       adj_combine_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, cg3(a->tmp[1]), as, g3(a->tmp[0]));
       // boundary: weights, then lam_{n-1}
-      adj_weights_kernel<<<(nelem + 127) / 128, 128, 0, a->stream>>>(a->dp, T, cg3(a->tmp[0]), g_amp, g_ph);
+      adj_weights_kernel<<<(nelem + 3) / 4, 128, 0, a->stream>>>(a->dp, T, cg3(a->tmp[0]), g_amp, g_ph);
       adj_boundary_kernel<<<grd, blk, 0, a->stream>>>(a->dp, cg3(a->tmp[0]), g3(li));
       if (n - 1 >= w.step_first && n - 1 <= w.step_last)
         adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(in[0], li[0], nx, w.i0, w.j0, w.ni, w.nj, coef);

@@ -483,14 +483,13 @@ fv_status enqueue_attempts(fv_handle *h, long long n) {
   return FV_OK;
 }
 
-// Four waves of resident CTAs, but no fewer than kMinRowsPerBlock strip-rows
-// per CTA (small grids). A warp of the step kernel is latency-bound, so an
-// SM runs at the speed of its resident warps: with one wave, SMs whose CTAs
-// finish early idle until the slowest CTA is done, while later waves keep
-// every SM full to the end (measured on 4096x2048: 4 waves 14% faster than
-// one, despite the extra halo rows of the shorter segments).
+// One wave of resident CTAs, but no fewer than kMinRowsPerBlock rows per
+// warp (small grids). Every warp of the step kernel streams the same number
+// of rows, so all CTAs of a wave finish together; a second wave would add
+// the warm-up rows of shorter segments, and a partial one (for instance 640
+// CTAs for 608 slots) nearly doubles the time.
 long long default_blocks(int max_resident, long long work) {
-  return std::max(1LL, std::min(4LL * max_resident, work / kMinRowsPerBlock));
+  return std::max(1LL, std::min((long long)max_resident, work / kMinRowsPerBlock));
 }
 
 fv_status reset_ctrl(fv_handle *h) {
@@ -687,8 +686,8 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "stream: %s", cudaGetErrorString(e)));
   h->stream = h->own_stream;
 
-  // launch shape: persistent CTAs, each streaming a balanced share of the
-  // (strip, row) space
+  // launch shape: persistent CTAs whose warps each stream a balanced share of
+  // the (window, row) space
   const int strip_cols = h->warps * kWarpCols;
   const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
   const long long work = (long long)nstrips * p->ny;
@@ -696,7 +695,9 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   h->max_resident = per_sm * prop.multiProcessorCount;
   long long blocks = default_blocks(h->max_resident, work);
   h->partials_cap = std::max(h->max_resident, 1) * 8;
-  // the fix-up launch: four CTAs per SM (its occupancy) take the marked chunks
+  // the fix-up launch: four CTAs per SM (two waves at its occupancy of two);
+  // warp w takes marked items w, w + W, ..., so warps past the last item exit
+  // at once
   const int fix_blocks = 4 * prop.multiProcessorCount;
   e = cudaMalloc(&h->partials, size_t(h->partials_cap + fix_blocks) * sizeof(float));
   if (e != cudaSuccess) return cleanup(fail(FV_CUDA_ERROR, "cudaMalloc partials: %s", cudaGetErrorString(e)));
@@ -995,6 +996,49 @@ fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts) {
                                             std::numeric_limits<float>::infinity());
   FV_CUDA(cudaGetLastError());
   return enqueue_attempts(h, nattempts);
+}
+
+fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_ms, float *attempt_ms) {
+  if (!h || nattempts < 1 || !step_kernel_ms || !attempt_ms) return fail(FV_BAD_ARG, "bad argument");
+  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nattempts,
+                                            std::numeric_limits<float>::infinity());
+  FV_CUDA(cudaGetLastError());
+  cudaEvent_t ev[4] = {};
+  for (int k = 0; k < 4; ++k) {
+    const cudaError_t e = cudaEventCreate(&ev[k]);
+    if (e != cudaSuccess) {
+      for (int j = 0; j < k; ++j) cudaEventDestroy(ev[j]);
+      return fail(FV_CUDA_ERROR, "cudaEventCreate: %s", cudaGetErrorString(e));
+    }
+  }
+  double step_sum = 0.0, att_sum = 0.0;
+  int rc = 0;
+  cudaError_t ec = cudaSuccess;
+  const int parts[3] = {kLaunchFrame, kLaunchStep, kLaunchFixFinal};
+  for (int n = 0; n < nattempts && rc == 0 && ec == cudaSuccess; ++n) {
+    ec = cudaEventRecord(ev[0], h->stream);
+    for (int k = 0; k < 3 && rc == 0 && ec == cudaSuccess; ++k) {
+      rc = launch(h, parts[k], h->args);
+      if (rc == 0 && k == 2 && h->collect) {  // the attempt's collector, as in launch_attempt
+        collect_kernel<<<1, 1024, 0, h->stream>>>(h->ctrl, h->args.state[0][0], h->args.state[1][0],
+                                                  h->params.nx, h->params.ny, h->coll);
+        rc = (int)cudaGetLastError();
+      }
+      if (rc == 0) ec = cudaEventRecord(ev[k + 1], h->stream);
+    }
+    if (rc == 0 && ec == cudaSuccess) ec = cudaEventSynchronize(ev[3]);
+    float ms_step = 0.f, ms_all = 0.f;
+    if (rc == 0 && ec == cudaSuccess) ec = cudaEventElapsedTime(&ms_step, ev[1], ev[2]);
+    if (rc == 0 && ec == cudaSuccess) ec = cudaEventElapsedTime(&ms_all, ev[0], ev[3]);
+    step_sum += ms_step;
+    att_sum += ms_all;
+  }
+  for (int k = 0; k < 4; ++k) cudaEventDestroy(ev[k]);
+  if (rc != 0) return fail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
+  if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "timing events: %s", cudaGetErrorString(ec));
+  *step_kernel_ms = float(step_sum / nattempts);
+  *attempt_ms = float(att_sum / nattempts);
+  return FV_OK;
 }
 
 fv_status fv_sync(fv_handle *h, fv_run_stats *out) {

@@ -89,6 +89,10 @@ constexpr int kFixRows = 8;
 // rewrites the stage rows of the chunks it recomputes. The adjoint's
 // segment replay records its linearisation points this way.
 constexpr int kStageRecord = -2;
+// The parts of an attempt (stage -1), for launching one at a time with
+// events between them (fv_time_attempts): the ghost-frame pre-pass, the
+// step kernel, and the fix-up and finalize launches.
+constexpr int kLaunchFrame = -3, kLaunchStep = -4, kLaunchFixFinal = -5;
 __host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }
@@ -118,14 +122,14 @@ struct StepArgs {
 };
 
 // One simulation of a batch: its parameters, buffers and control block,
-// and where its strip-rows start in the batch's concatenated work.
+// and where its window-rows start in the batch's concatenated work.
 struct BatchInst {
   DevParams p;
   float *state[2][3];
   float *frame[3];
   Ctrl *ctrl;
-  int64_t work_begin;     // first strip-row of this instance in the batch
-  int64_t work;           // nstrips * ny
+  int64_t work_begin;     // first window-row of this instance in the batch
+  int64_t work;           // windows * ny (windows of kWarpCols output columns)
   int64_t fix_base;       // first chunk id of this instance in the fix-up scratch
 };
 
@@ -139,7 +143,7 @@ struct BatchArgs {
   uint32_t *fix;          // fix-up scratch, zero between attempts
   int32_t n;
   int32_t nblocks;
-  int64_t work;           // total strip-rows
+  int64_t work;           // total window-rows
   int64_t fix_chunks;     // total chunks over all instances
   int32_t max_frame;      // largest frame pre-pass work of an instance
   int32_t fix_blocks;     // CTAs of the fix-up launch

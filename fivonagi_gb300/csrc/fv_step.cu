@@ -785,14 +785,19 @@ struct BatchMarker {
 // the simulation's buffers and parameters come from global memory, and at
 // four the kernel would spill (measured: three is faster).
 __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
-  __shared__ float red[kWarps];
-  __shared__ int neg_any;
-  const int warp = threadIdx.x >> 5;
+  // Each warp streams a balanced share of the batch's concatenated
+  // (simulation, window, row) space and folds its CFL maximum and
+  // negative-eigenvalue flag into each simulation it touched.
   const long long W = b.work;
-  const long long bid = blockIdx.x;
-  const long long s0 = bid * W / b.nblocks, s1 = (bid + 1) * W / b.nblocks;
-  int k = 0;
-  while (k < b.n - 1 && b.inst[k + 1].work_begin <= s0) ++k;
+  const long long G = (long long)b.nblocks * kWarps;
+  const long long g = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const long long s0 = g * W / G, s1 = (g + 1) * W / G;
+  int lo = 0, hi = b.n - 1;  // the simulation holding s0: last with work_begin <= s0
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (b.inst[mid].work_begin <= s0) lo = mid; else hi = mid - 1;
+  }
+  int k = lo;
   long long pos = s0;
   while (pos < s1 && k < b.n) {
     const BatchInst &I = b.inst[k];
@@ -810,34 +815,25 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
       const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
       float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
       const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
-      if (threadIdx.x == 0) neg_any = 0;
-      __syncthreads();
       float cmax = 0.0f;
       bool neg = false;
       for (long long q = pos; q < seg_end;) {
         const long long rel = q - kb;
-        const int strip = (int)(rel / p.ny);
-        const int y0 = (int)(rel - (long long)strip * p.ny);
+        const int win = (int)(rel / p.ny);
+        const int y0 = (int)(rel - (long long)win * p.ny);
         const long long left = seg_end - q;
         const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
-        const int xw = strip * kStripCols + warp * kWarpCols;
-        if (xw < p.nx) {
-          BatchMarker mk{b, k, -1};
-          stream_window<-1, DivFma>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
-        }
+        BatchMarker mk{b, k, -1};
+        stream_window<-1, DivFma>(p, in, frame, out, win * kWarpCols, y0, y1, dt, T, mdx, mdy, shx, shy, cmax,
+                                  neg, mk);
         q += y1 - y0;
       }
       for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
-      if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) neg_any = 1;
-      if ((threadIdx.x & 31) == 0) red[warp] = cmax;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        float m = red[0];
-        for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
-        atomicMax(b.cfl_bits + k, __float_as_uint(m));
-        if (neg_any) atomicExch(b.neg + k, 1);
+      const bool wneg = __any_sync(0xffffffffu, neg);
+      if ((threadIdx.x & 31) == 0) {
+        atomicMax(b.cfl_bits + k, __float_as_uint(cmax));
+        if (wneg) atomicExch(b.neg + k, 1);
       }
-      __syncthreads();
     }
     pos = seg_end;
     ++k;
@@ -940,9 +936,16 @@ template <int STAGE> static void *kernel_ptr() { return (void *)step_kernel<STAG
 static int launch_impl(const StepArgs &a, int stage, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   const int ftotal = 4 * a.p.nx + 4 * (a.p.ny - 4);
-  ghost_frame_kernel<<<(ftotal + 255) / 256, 256, 0, st>>>(a, stage < 0 ? 1 : 0);
+  if (stage != kLaunchStep && stage != kLaunchFixFinal)
+    ghost_frame_kernel<<<(ftotal + 255) / 256, 256, 0, st>>>(a, stage < 0 ? 1 : 0);
   dim3 grid(a.nblocks), block(kThreads);
   switch (stage) {
+    case kLaunchFrame: break;
+    case kLaunchStep: step_kernel<-1><<<grid, block, 0, st>>>(a); break;
+    case kLaunchFixFinal:
+      fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);
+      finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
+      break;
     case -1:
       step_kernel<-1><<<grid, block, 0, st>>>(a);
       fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);

@@ -182,6 +182,14 @@ class Simulation:
     def launch_attempts(self, n: int) -> None:
         check(self.lib.fv_launch_attempts(self.h, int(n)), "fv_launch_attempts")
 
+    def time_attempts(self, n: int) -> tuple[float, float]:
+        """(step kernel ms, attempt ms), averaged over n attempts launched
+        one at a time with CUDA events between their launches
+        (fv_time_attempts)."""
+        sk, at = C.c_float(), C.c_float()
+        check(self.lib.fv_time_attempts(self.h, int(n), C.byref(sk), C.byref(at)), "fv_time_attempts")
+        return sk.value, at.value
+
     def sync(self) -> dict:
         st = FvRunStats()
         check(self.lib.fv_sync(self.h, C.byref(st)), "fv_sync")

@@ -275,9 +275,18 @@ fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out);
 fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts);
 fv_status fv_sync(fv_handle *h, fv_run_stats *out);
 
+/* Runs nattempts attempts one at a time, without graph capture, with CUDA
+ * events on the handle's stream between the attempt's launches, and returns
+ * the step kernel's average duration and the whole attempt's, in ms.
+ * Synchronises. For roofline measurements of the step kernel alone. No
+ * reference counterpart: the reference times nothing on the device. */
+fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_ms,
+                           float *attempt_ms);
+
 /* Launch shape of the step kernel, for the autotuner: `blocks` persistent
- * CTAs share the grid's (strip, row) work evenly; 0 restores the default
- * (four waves of resident CTAs, at most 8 waves). fv_get_launch reports the current value and
+ * CTAs of 4 warps, each warp streaming an even share of the grid's
+ * (26-column window, row) work; 0 restores the default (one wave of
+ * resident CTAs; at most 8 waves). fv_get_launch reports the current value and
  * how many CTAs fit on the device at once. No reference counterpart: the
  * reference launches one thread per cell (common/main.cu:252-253). */
 fv_status fv_set_launch(fv_handle *h, int32_t blocks);
@@ -316,7 +325,9 @@ fv_status fv_batch_run(fv_batch *b, int64_t nsteps, fv_run_stats *out);
  * fv_batch_sync waits and reports. */
 fv_status fv_batch_launch_attempts(fv_batch *b, int64_t nattempts);
 fv_status fv_batch_sync(fv_batch *b, fv_run_stats *out);
-/* CTAs of the batch launch (0 = default), for the autotuner. */
+/* CTAs of the batch launch, each warp streaming an even share of the
+ * concatenated (simulation, window, row) work (0 = default: eight waves of
+ * resident CTAs, at least 32 rows per warp). */
 fv_status fv_batch_set_launch(fv_batch *b, int32_t blocks);
 fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_resident);
 

@@ -270,3 +270,29 @@ def test_phased_array_matches_oracle(nx, ny):
         assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
     assert np.abs(g[0]).max() > 1e-3  # the source reached the grid
     sim.close()
+
+
+@pytest.mark.parametrize("blocks", [0, 7])
+def test_timed_attempts_match_ordinary_attempts(blocks):
+    """fv_time_attempts launches an attempt's kernels one at a time with
+    events between them; the state it leaves is the one the same number of
+    ordinary (graph-captured) attempts leaves, and the step kernel's time
+    is part of the attempt's."""
+    p = small_params(3, 300, 130)
+    sims = [Simulation(p), Simulation(p)]
+    for s in sims:
+        s.set_launch(blocks)
+        s.init_state()
+        s.run(5)
+    n = 40
+    sims[0].launch_attempts(n)
+    st0 = sims[0].sync()
+    step_ms, attempt_ms = sims[1].time_attempts(n)
+    st1 = sims[1].stats()
+    assert 0.0 < step_ms < attempt_ms
+    assert (st0["n"], st0["accepted"], st0["rejected"]) == (st1["n"], st1["accepted"], st1["rejected"])
+    a, b = sims[0].get_state(), sims[1].get_state()
+    for f in range(3):
+        assert same_values(a[f], b[f])
+    for s in sims:
+        s.close()
