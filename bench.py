@@ -60,6 +60,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest of every rank's x (the job's time is its slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells: int, steps_per_rank: int, world: int, ms: float) -> float:
+    """Gcell-updates/s of the whole job: every rank advances its own replica
+    by steps_per_rank steps; ms is the slowest rank's time."""
+    return cells * steps_per_rank * world / (ms * 1e-3) / 1e9
+
+
 class ClockSampler:
     """nvidia-smi clock and throttle-reason samples during the timed region."""
 
@@ -250,11 +266,9 @@ def run_gpu(args):
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
     accepted = int(st["accepted"])
-    value = cells * accepted * world / (ms * 1e-3) / 1e9
+    value = replica_throughput(cells, accepted, world, ms)
     per_launch_ms = ms / max(1, accepted + int(st["rejected"]))
 
     # ---- one step timed alone after an L2 flush, as a cross-check
@@ -300,13 +314,11 @@ def run_gpu(args):
     sim.close()
     e2e_s = t1 - t0
     if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dev)
     state_bytes = 3 * cells * 4
     ctrl_bytes = C.sizeof(_abi.FvRunStats)
     e2e = {
-        "value": cells * e2e_steps * world / e2e_s / 1e9,
+        "value": replica_throughput(cells, e2e_steps, world, e2e_s * 1e3),
         "unit": "Gcell-updates/s",
         "steps": e2e_steps,
         "h2d_bytes_per_step": state_bytes / e2e_steps,
