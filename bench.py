@@ -236,13 +236,22 @@ def run_gpu(args):
     params = workload_params(exact)
     cells = params.nx * params.ny
 
-    # ---- launch shape from the autotuner (cached; outside every timed region),
-    # or as given (--blocks: few launches before a profiler's capture)
-    blocks = args.blocks if args.blocks > 0 else autotune.tune(params)
+    # ---- launch shape and division from the autotuner (cached; outside every
+    # timed region), or as given (--blocks/--division: few launches before a
+    # profiler's capture)
+    DIVISIONS = {"default": _abi.FV_DIVISION_DEFAULT, "fma": _abi.FV_DIVISION_FMA, "exact": _abi.FV_DIVISION_EXACT}
+    if args.blocks > 0:
+        blocks, division = args.blocks, DIVISIONS[args.division]
+    else:
+        blocks, division = autotune.tune(params)
+        if args.division != "default":
+            division = DIVISIONS[args.division]
 
     # ---- device-timed throughput (state resident in HBM)
     sim = Simulation(params)
     sim.set_launch(blocks)
+    sim.set_division(division)
+    division_used = "exact" if sim.get_division() == _abi.FV_DIVISION_EXACT else "fma"
     sim.init_state()
     stream = torch.cuda.Stream(device=dev)
     sim.set_stream(stream.cuda_stream)
@@ -297,6 +306,7 @@ def run_gpu(args):
     # ---- end to end through the C ABI with pinned host buffers
     sim = Simulation(params)
     sim.set_launch(blocks)
+    sim.set_division(division)
     sim.set_stream(stream.cuda_stream)
     u0 = torch.zeros((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
     u_out = torch.empty((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
@@ -377,6 +387,7 @@ def run_gpu(args):
                   "writing 258 MB",
             "parallelism": "replicas" if world > 1 else "single GPU",
             "ctas_per_launch": blocks,
+            "step_division": division_used,
         },
         "roofline": roofline,
         "e2e": e2e,
@@ -434,7 +445,9 @@ def run_batched(args):
     acc_seq = 0
     for p in plist:
         sim = Simulation(p)
-        sim.set_launch(autotune.tune(p, steps=20))
+        b, m = autotune.tune(p, steps=20)
+        sim.set_launch(b)
+        sim.set_division(m)
         sim.set_stream(stream.cuda_stream)
         sim.init_state()
         sim.run(max(args.warmup, 3))
@@ -652,6 +665,9 @@ def main():
                          "case for a profiler's launch list)")
     ap.add_argument("--blocks", type=int, default=0,
                     help="plain workload: CTAs per step launch instead of the autotuner's choice")
+    ap.add_argument("--division", choices=["default", "fma", "exact"], default="default",
+                    help="plain workload: the step kernel's division instead of the autotuner's (or, with "
+                         "--blocks, the library default's) choice")
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

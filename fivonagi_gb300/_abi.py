@@ -42,6 +42,11 @@ FV_APP_TAYLOR_ANGLE_XY = 1
 FV_APP_PLANE_WAVE = 2
 FV_APP_FOCUSED_BEAM = 3
 FV_APP_PHASED_ARRAY = 4
+
+# division in the step kernel (fv_set_division)
+FV_DIVISION_DEFAULT = -1
+FV_DIVISION_FMA = 0
+FV_DIVISION_EXACT = 1
 APP_NAMES = {
     "hifu-beam": FV_APP_HIFU_BEAM,
     "taylor-angle-xy": FV_APP_TAYLOR_ANGLE_XY,
@@ -210,6 +215,8 @@ PROTOTYPES = {
     "fv_run_until": (C.c_int, [_P, C.c_double, C.POINTER(FvRunStats)]),
     "fv_launch_attempts": (C.c_int, [_P, C.c_int64]),
     "fv_time_attempts": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "fv_set_division": (C.c_int, [_P, C.c_int32]),
+    "fv_get_division": (C.c_int, [_P, _P]),
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "fv_set_launch": (C.c_int, [_P, C.c_int32]),

@@ -1,10 +1,13 @@
 """Launch-shape autotuner for the step kernel.
 
-The step kernel's only free launch parameter is the number of persistent
-CTAs that share the grid's (column strip, row) work (fv_set_launch). More
-waves keep every SM full to the end, but shorter row segments repeat the
-8-row warm-up/drain of the streaming loop, so the best count depends on the
-grid size. `tune` times a few candidates, in waves of the CTAs resident at
+The step kernel has two free launch parameters: the number of persistent
+CTAs whose warps share the grid's (window, row) work (fv_set_launch), and
+the division it computes with (fv_set_division: FMA division with a fix-up
+pass, or exact division with no fix-up work; the results are the same bit
+for bit). More waves keep every SM full to the end but repeat the streaming
+loop's warm-up rows on shorter segments; exact division costs the step
+kernel a few percent and saves the fix-up pass. The best pair depends on
+the grid size. `tune` times each pair, in waves of the CTAs resident at
 once, on a scratch copy of the simulation, and caches the winner per
 (device, grid, variant) in a JSON file next to the library.
 """
@@ -40,8 +43,9 @@ def _store(d: dict) -> None:
     os.replace(tmp, CACHE)
 
 
-def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> int:
-    """Best CTA count for `params` on the current device (cached)."""
+def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> tuple[int, int]:
+    """Best (CTA count, division mode) for `params` on the current device
+    (cached)."""
     import torch
 
     from .solver import Simulation
@@ -49,8 +53,8 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> int:
     device = torch.cuda.get_device_name()
     key = _key(params, device)
     cache = _load()
-    if key in cache and not refresh:
-        return int(cache[key]["blocks"])
+    if key in cache and not refresh and "division" in cache[key]:
+        return int(cache[key]["blocks"]), int(cache[key]["division"])
     sim = Simulation(params)
     try:
         sim.init_state()
@@ -59,32 +63,36 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> int:
         sim.run(10)
         _, resident = sim.get_launch()
         results = {}
-        for w in WAVES:
-            b = w * resident
-            try:
-                sim.set_launch(b)
-            except _abi.FvError:
-                continue
-            sim.run(4)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            sim.launch_attempts(steps)
-            e1.record(stream)
-            stream.synchronize()
-            sim.sync()
-            results[b] = e0.elapsed_time(e1) / steps
+        for mode in (_abi.FV_DIVISION_FMA, _abi.FV_DIVISION_EXACT):
+            sim.set_division(mode)
+            for w in WAVES:
+                b = w * resident
+                try:
+                    sim.set_launch(b)
+                except _abi.FvError:
+                    continue
+                sim.run(4)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sim.launch_attempts(steps)
+                e1.record(stream)
+                stream.synchronize()
+                sim.sync()
+                results[(b, mode)] = e0.elapsed_time(e1) / steps
         best = min(results, key=results.get)
     finally:
         sim.close()
-    cache[key] = {"blocks": best, "ms_per_step": results[best],
-                  "candidates": {str(k): v for k, v in sorted(results.items())}}
+    cache[key] = {"blocks": best[0], "division": best[1], "ms_per_step": results[best],
+                  "candidates": {f"{b}/{'exact' if m else 'fma'}": v for (b, m), v in sorted(results.items())}}
     _store(cache)
     return best
 
 
-def apply(sim, refresh: bool = False) -> int:
-    """Tune for `sim`'s parameters and set its launch shape; returns the CTAs."""
-    b = tune(sim.params, refresh=refresh)
+def apply(sim, refresh: bool = False) -> tuple[int, int]:
+    """Tune for `sim`'s parameters and set its launch shape and division;
+    returns (CTAs, division mode)."""
+    b, m = tune(sim.params, refresh=refresh)
     sim.set_launch(b)
-    return b
+    sim.set_division(m)
+    return b, m

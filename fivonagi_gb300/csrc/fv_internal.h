@@ -93,6 +93,10 @@ constexpr int kStageRecord = -2;
 // events between them (fv_time_attempts): the ghost-frame pre-pass, the
 // step kernel, and the fix-up and finalize launches.
 constexpr int kLaunchFrame = -3, kLaunchStep = -4, kLaunchFixFinal = -5;
+// A full attempt whose step kernel divides exactly (DivExact) instead of
+// with FMA division: the fix-up pass then meets only operands out of
+// range. Chosen by StepArgs::div_exact.
+constexpr int kStageExactDiv = -6;
 __host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }
@@ -118,7 +122,8 @@ struct StepArgs {
   int32_t nblocks;        // CTAs of the launch
   int64_t work;           // nstrips * ny: strip-rows (sizes the default launch)
   int32_t fix_blocks;     // CTAs of the fix-up launch
-  int32_t pad0;
+  int32_t div_exact;      // attempts (-1, kLaunchStep) run the step kernel with exact
+                          // division (kStageExactDiv) instead of FMA division
 };
 
 // One simulation of a batch: its parameters, buffers and control block,

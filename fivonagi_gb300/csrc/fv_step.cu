@@ -573,7 +573,13 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
   }
   const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
-  using DP = typename std::conditional<(STAGE < 0), DivFma, DivIEEE>::type;
+  // Exact division (DivExact) for kStageExactDiv and for the adjoint's
+  // stage-recording replays: the fix-up pass then has no work. It costs
+  // the step kernel 2-5% more than FMA division; whether the fix-up pass it
+  // saves is worth more depends on the grid (see fv_set_division). The
+  // replays gain 3% per backward step at 1024x1024.
+  using DP = typename std::conditional<(STAGE == kStageRecord || STAGE == kStageExactDiv), DivExact,
+                                       typename std::conditional<(STAGE < 0), DivFma, DivIEEE>::type>::type;
 
   const int warp = threadIdx.x >> 5;
   const int ny = a.p.ny;
@@ -941,13 +947,21 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
   dim3 grid(a.nblocks), block(kThreads);
   switch (stage) {
     case kLaunchFrame: break;
-    case kLaunchStep: step_kernel<-1><<<grid, block, 0, st>>>(a); break;
+    case kLaunchStep:
+      if (a.div_exact)
+        step_kernel<kStageExactDiv><<<grid, block, 0, st>>>(a);
+      else
+        step_kernel<-1><<<grid, block, 0, st>>>(a);
+      break;
     case kLaunchFixFinal:
       fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);
       finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;
     case -1:
-      step_kernel<-1><<<grid, block, 0, st>>>(a);
+      if (a.div_exact)
+        step_kernel<kStageExactDiv><<<grid, block, 0, st>>>(a);
+      else
+        step_kernel<-1><<<grid, block, 0, st>>>(a);
       fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);
       finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;

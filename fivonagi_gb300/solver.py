@@ -205,6 +205,16 @@ class Simulation:
         check(self.lib.fv_get_launch(self.h, C.byref(b), C.byref(m)), "fv_get_launch")
         return b.value, m.value
 
+    def set_division(self, mode: int) -> None:
+        """Division in the step kernel (fv_set_division): _abi.FV_DIVISION_FMA,
+        FV_DIVISION_EXACT or FV_DIVISION_DEFAULT; results are the same."""
+        check(self.lib.fv_set_division(self.h, int(mode)), "fv_set_division")
+
+    def get_division(self) -> int:
+        m = C.c_int32()
+        check(self.lib.fv_get_division(self.h, C.byref(m)), "fv_get_division")
+        return m.value
+
     def debug_step(self, stage: int):
         """One step of the current state stopped after `stage` (no commit)."""
         out = [np.empty(self.shape, np.float32) for _ in range(3)]

@@ -292,6 +292,21 @@ fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_m
 fv_status fv_set_launch(fv_handle *h, int32_t blocks);
 fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident);
 
+/* Division in the step kernel, for the autotuner. Both give the same
+ * results bit for bit (IEEE-equal quotients everywhere):
+ *   FV_DIVISION_FMA: FMA-based division, with a fix-up pass that recomputes
+ *     the few rows where its operands leave its proven range (subnormal
+ *     quotients) with exact division;
+ *   FV_DIVISION_EXACT: exact division in the step kernel itself, slower per
+ *     row, with no fix-up work;
+ *   FV_DIVISION_DEFAULT: EXACT from 2^21 cells up, FMA below.
+ * No reference counterpart: the reference uses the compiler's division. */
+#define FV_DIVISION_DEFAULT (-1)
+#define FV_DIVISION_FMA 0
+#define FV_DIVISION_EXACT 1
+fv_status fv_set_division(fv_handle *h, int32_t mode);
+fv_status fv_get_division(fv_handle *h, int32_t *mode);
+
 /* One step of the current state, stopped after `stage`; writes the stage's
  * full grid to u1/u2/u3 (host pointers) and leaves the handle's state,
  * dt, T and n unchanged. For per-phase parity tests. */

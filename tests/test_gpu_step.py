@@ -12,7 +12,7 @@ import pytest
 
 from fivonagi_gb300 import Simulation, _abi
 from oracle.oracle import OracleSim
-from tests.helpers import perturbed, rel_l2, same_values, small_params
+from tests.helpers import array_weights, perturbed, rel_l2, same_values, small_params
 
 pytestmark = pytest.mark.gpu
 
@@ -272,8 +272,8 @@ def test_phased_array_matches_oracle(nx, ny):
     sim.close()
 
 
-@pytest.mark.parametrize("blocks", [0, 7])
-def test_timed_attempts_match_ordinary_attempts(blocks):
+@pytest.mark.parametrize("blocks,division", [(0, _abi.FV_DIVISION_FMA), (7, _abi.FV_DIVISION_EXACT)])
+def test_timed_attempts_match_ordinary_attempts(blocks, division):
     """fv_time_attempts launches an attempt's kernels one at a time with
     events between them; the state it leaves is the one the same number of
     ordinary (graph-captured) attempts leaves, and the step kernel's time
@@ -282,6 +282,7 @@ def test_timed_attempts_match_ordinary_attempts(blocks):
     sims = [Simulation(p), Simulation(p)]
     for s in sims:
         s.set_launch(blocks)
+        s.set_division(division)
         s.init_state()
         s.run(5)
     n = 40
@@ -296,3 +297,41 @@ def test_timed_attempts_match_ordinary_attempts(blocks):
         assert same_values(a[f], b[f])
     for s in sims:
         s.close()
+
+
+@pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (0, 130, 300), (1, 104, 64), (4, 96, 64)])
+def test_division_modes_give_the_same_results(app, nx, ny):
+    """FMA division with its fix-up pass and exact division in the step
+    kernel both give IEEE quotients: the runs agree bit for bit (the FMA
+    mode is the one the oracle parity tests run on small grids)."""
+    p = small_params(app, nx, ny)
+    out = []
+    for mode in (_abi.FV_DIVISION_FMA, _abi.FV_DIVISION_EXACT):
+        sim = Simulation(p)
+        if app == 4:
+            sim.set_array_weights(*array_weights(p.array_elems, 3, p.ampl))
+        sim.set_division(mode)
+        assert sim.get_division() == mode
+        sim.init_state()
+        st = sim.run(80)
+        out.append((st["n"], st["T"], sim.get_state()))
+        sim.close()
+    (n0, t0, a), (n1, t1, b) = out
+    assert (n0, t0) == (n1, t1)
+    for f in range(3):
+        assert same_values(a[f], b[f])
+
+
+def test_default_division_depends_on_the_grid():
+    small = Simulation(small_params(3, 300, 130))
+    large = Simulation(small_params(3, 2048, 1024))
+    try:
+        assert small.get_division() == _abi.FV_DIVISION_FMA
+        assert large.get_division() == _abi.FV_DIVISION_EXACT
+        large.set_division(_abi.FV_DIVISION_FMA)
+        assert large.get_division() == _abi.FV_DIVISION_FMA
+        large.set_division(_abi.FV_DIVISION_DEFAULT)
+        assert large.get_division() == _abi.FV_DIVISION_EXACT
+    finally:
+        small.close()
+        large.close()
