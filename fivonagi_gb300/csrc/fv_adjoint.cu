@@ -22,11 +22,11 @@
 // states; each replayed attempt also records its stage grids B, Y, X (the
 // step kernel writes them as it goes, kStageRecord), the linearisation
 // points of the reverse step. Then walk the segment backwards. A reverse
-// step runs grid-wide reverse kernels: diffusion, x sweep, y sweep (three
-// kernels each: waves, interface adjoints, per-cell gather), boundary
-// (ghost cells back to the cells they copy, and the source cells to the
-// weights).
-// Memory: 3 (N / C) + 12 C + ~40 grids; C = ceil(sqrt(N)) by default.
+// step runs the reverse kernels: diffusion; one fused kernel per sweep
+// (waves, limiter reverse, solve reverse and the per-cell gather, with the
+// sweep's neighbours in registers and warp shuffles); boundary (ghost cells
+// back to the cells they copy, and the source cells to the weights).
+// Memory: 3 (N / C) + 12 C + ~21 grids; C = ceil(sqrt(N)) by default.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,12 +51,6 @@ struct G3 {
 };
 struct CG3 {
   const float *f[3];
-};
-struct WaveStore {
-  float *w[10];  // s1 s2 s3 w11 w21 w31 w12 w22 w32 w33, per interface (at its 'a' cell)
-};
-struct AdjStore {
-  float *g[6];  // ga (the interface's 'a' cell) then gb (its 'b' cell), local frame
 };
 
 // Records of the forward run, written by one-thread kernels.
@@ -213,131 +207,196 @@ __global__ void adj_diffusion_kernel(DevParams p, float dt, CG3 s2, CG3 lo, G3 l
   li.f[2][o] = lo.f[2][o] + fdiv(gvy, rho);
 }
 
-// Local frame of a sweep: component 1 = u1; x sweep (dir 0): normal = u2,
-// transverse = u3; y sweep (dir 1): normal = u3, transverse = u2
+// Local frame of a sweep: component 1 = u1; x sweep: normal = u2,
+// transverse = u3; y sweep: normal = u3, transverse = u2
 // (apps/na/fv.h:489-493).
-__device__ __forceinline__ void local3(const CG3 &g, int dir, size_t o, float &q1, float &qn, float &qt) {
-  q1 = g.f[0][o];
-  qn = g.f[dir == 0 ? 1 : 2][o];
-  qt = g.f[dir == 0 ? 2 : 1][o];
+__device__ __forceinline__ Adj3 load_local(const CG3 &g, bool xsweep, size_t o) {
+  return Adj3{g.f[0][o], g.f[xsweep ? 1 : 2][o], g.f[xsweep ? 2 : 1][o]};
+}
+__device__ __forceinline__ void store_local(const G3 &g, bool xsweep, size_t o, const Adj3 &v) {
+  g.f[0][o] = v.q1;
+  g.f[xsweep ? 1 : 2][o] = v.qn;
+  g.f[xsweep ? 2 : 1][o] = v.qt;
 }
 
-__device__ __forceinline__ WaveN load_wave(const WaveStore &ws, size_t o) {
-  WaveN w;
-  w.s1 = ws.w[0][o]; w.s2 = ws.w[1][o]; w.s3 = ws.w[2][o];
-  w.w11 = ws.w[3][o]; w.w21 = ws.w[4][o]; w.w31 = ws.w[5][o];
-  w.w12 = ws.w[6][o]; w.w22 = ws.w[7][o]; w.w32 = ws.w[8][o];
-  w.w33 = ws.w[9][o];
-  return w;
+__device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ Adj3 shup(const Adj3 &v) { return Adj3{shup(v.q1), shup(v.qn), shup(v.qt)}; }
+__device__ __forceinline__ Adj3 shdn(const Adj3 &v) { return Adj3{shdn(v.q1), shdn(v.qn), shdn(v.qt)}; }
+__device__ __forceinline__ WaveN shup(const WaveN &w) {
+  return WaveN{shup(w.s1), shup(w.s2), shup(w.s3), shup(w.w11), shup(w.w21),
+               shup(w.w31), shup(w.w12), shup(w.w22), shup(w.w32), shup(w.w33)};
+}
+__device__ __forceinline__ WaveN shdn(const WaveN &w) {
+  return WaveN{shdn(w.s1), shdn(w.s2), shdn(w.s3), shdn(w.w11), shdn(w.w21),
+               shdn(w.w31), shdn(w.w12), shdn(w.w22), shdn(w.w32), shdn(w.w33)};
+}
+__device__ __forceinline__ WaveAdj shup(const WaveAdj &w) {
+  return WaveAdj{shup(w.s1), shup(w.s2), shup(w.s3), shup(w.w11), shup(w.w21),
+                 shup(w.w31), shup(w.w12), shup(w.w22), shup(w.w32), shup(w.w33)};
+}
+__device__ __forceinline__ WaveAdj shdn(const WaveAdj &w) {
+  return WaveAdj{shdn(w.s1), shdn(w.s2), shdn(w.s3), shdn(w.w11), shdn(w.w21),
+                 shdn(w.w31), shdn(w.w12), shdn(w.w22), shdn(w.w32), shdn(w.w33)};
+}
+__device__ __forceinline__ void add_to(WaveAdj &a, const WaveAdj &b) {
+  a.s1 += b.s1; a.s2 += b.s2; a.s3 += b.s3;
+  a.w11 += b.w11; a.w21 += b.w21; a.w31 += b.w31;
+  a.w12 += b.w12; a.w22 += b.w22; a.w32 += b.w32; a.w33 += b.w33;
 }
 
-// Waves and speeds at every interface of a sweep (the interface between a
-// cell and its predecessor along the sweep; none for the first cell).
-__global__ void adj_waves_kernel(DevParams p, int dir, float dt, CG3 s, WaveStore ws) {
-  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
-  const int nx = p.nx, ny = p.ny;
-  if (i >= nx || j >= ny) return;
-  const size_t o = size_t(i) + size_t(j) * nx;
-  const int k = dir == 0 ? i : j;
+// Waves and speeds of the solve between cell a and its predecessor b along
+// the sweep (zero where the interface does not exist).
+__device__ __forceinline__ WaveN sweep_waves(const Adj3 &sa, const Adj3 &sb, float two_bm1, float dtx, bool exists) {
   WaveN w{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  if (k >= 1) {
-    const size_t b = dir == 0 ? o - 1 : o - size_t(nx);
-    float q1a, qna, qta, q1b, qnb, qtb;
-    local3(s, dir, o, q1a, qna, qta);
-    local3(s, dir, b, q1b, qnb, qtb);
-    const float ra = q1a + 1.0f, rb = q1b + 1.0f;
-    const float dtx = dt / (dir == 0 ? p.dx : p.dy);
+  if (exists) {
+    const float ra = sa.q1 + 1.0f, rb = sb.q1 + 1.0f;
     float cfl = 0.0f;
     Fluct f;
     DivFast fast;
-    riemann(ra, qna, qta, fdiv(qna, ra), fdiv(qta, ra), rb, qnb, qtb, fdiv(qnb, rb), fdiv(qtb, rb),
-            2.0f * (p.beta - 1.0f), dtx, cfl, w, f, fast);
+    riemann(ra, sa.qn, sa.qt, fdiv(sa.qn, ra), fdiv(sa.qt, ra), rb, sb.qn, sb.qt, fdiv(sb.qn, rb), fdiv(sb.qt, rb),
+            two_bm1, dtx, cfl, w, f, fast);
   }
-  ws.w[0][o] = w.s1; ws.w[1][o] = w.s2; ws.w[2][o] = w.s3;
-  ws.w[3][o] = w.w11; ws.w[4][o] = w.w21; ws.w[5][o] = w.w31;
-  ws.w[6][o] = w.w12; ws.w[7][o] = w.w22; ws.w[8][o] = w.w32;
-  ws.w[9][o] = w.w33;
+  return w;
 }
 
-// Adjoints of the two cells of each interface. The sweep updates interior
-// cell R as u_R - dtx (apdq_R + amdq_{R+1}) - dtx (F_{R+1} - F_R), F_k the
-// limited correction flux at interface k (step_x/_y, writeLimiters_x/_y,
-// apps/na/fv.h:384-499, 933-1054). With mu the output adjoint on interior
-// cells (0 elsewhere): d apdq_k = -dtx mu_k, d amdq_k = -dtx mu_{k-1},
-// d F_k = dtx (mu_k - mu_{k-1}). The waves at k feed the corrections at
-// k-1, k, k+1, whose reverses are gathered here; then the Riemann solve's
-// reverse gives the two cells' adjoints.
-__global__ void adj_interface_kernel(DevParams p, int dir, float dt, CG3 s, CG3 lo, WaveStore ws,
-                                     AdjStore as) {
-  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+__device__ __forceinline__ Adj3 masked(const Adj3 &v, bool keep) {
+  return keep ? v : Adj3{0.f, 0.f, 0.f};
+}
+
+// The reverse of one sweep, whose forward updates interior cell k as
+//   u_k - dtx (apdq_k + amdq_{k+1}) - dtx (F_{k+1} - F_k),
+// F_k the limited correction flux at interface k (step_x/_y and
+// writeLimiters_x/_y, apps/na/fv.h:384-499, 933-1054). With mu the output
+// adjoint on interior cells (0 elsewhere): d apdq_k = -dtx mu_k,
+// d amdq_k = -dtx mu_{k-1}, d F_k = dtx (mu_k - mu_{k-1}). Per interface k:
+// the solve's waves; the limiter's reverse at k, whose adjoints go to the
+// waves at k-1, k, k+1; the waves' adjoint at k, gathered from the limiter
+// reverses at k-1, k, k+1; the solve's reverse, giving the adjoints of its
+// two cells (ga to cell k, gb to cell k-1); and the sweep's input adjoint
+// lo_k + ga_k + gb_{k+1}. Interface k exists for 1 <= k <= n-1.
+//
+// x sweep: lanes along a row, 26 output columns per warp with a 3-column
+// halo each side (the columns of the step kernel's windows); neighbours are
+// neighbouring lanes. A warp takes (window, row) pairs, consecutive warps
+// neighbouring windows of one row.
+__global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt, CG3 s, CG3 lo, G3 li) {
   const int nx = p.nx, ny = p.ny;
-  if (i >= nx || j >= ny) return;
-  const size_t o = size_t(i) + size_t(j) * nx;
-  const int k = dir == 0 ? i : j;
-  const int n = dir == 0 ? nx : ny;
-  const long long step = dir == 0 ? 1 : nx;
-  Adj3 ga{0.f, 0.f, 0.f}, gb{0.f, 0.f, 0.f};
-  if (k >= 1) {
-    const float dtx = dt / (dir == 0 ? p.dx : p.dy);
-    auto mu = [&](int kk) {
-      Adj3 m{0.f, 0.f, 0.f};
-      const int ii = dir == 0 ? kk : i, jj = dir == 0 ? j : kk;
-      if (kk >= 0 && kk < n && interior(p, ii, jj)) {
-        local3(lo, dir, size_t(ii) + size_t(jj) * nx, m.q1, m.qn, m.qt);
-      }
-      return m;
-    };
-    auto wave = [&](int kk) {
-      if (kk < 1 || kk > n - 1) return WaveN{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      return load_wave(ws, size_t((long long)o + (long long)(kk - k) * step));
-    };
-    const Adj3 mm2 = mu(k - 2), mm1 = mu(k - 1), m0 = mu(k), mp1 = mu(k + 1);
-    const WaveN wm2 = wave(k - 2), wm1 = wave(k - 1), w0 = wave(k), wp1 = wave(k + 1), wp2 = wave(k + 2);
-    WaveAdj gw, dm, dz, dp;
-    zero(gw); zero(dm); zero(dz); zero(dp);
-    // correction at k-1 (waves k-2, k-1, k): its right-neighbour part
-    if (k - 1 >= 1)
-      correction_adj(wm2, wm1, w0, dtx, dtx * (mm1.q1 - mm2.q1), dtx * (mm1.qn - mm2.qn),
-                     dtx * (mm1.qt - mm2.qt), dm, dz, gw);
-    // correction at k (waves k-1, k, k+1): its own part
-    correction_adj(wm1, w0, wp1, dtx, dtx * (m0.q1 - mm1.q1), dtx * (m0.qn - mm1.qn), dtx * (m0.qt - mm1.qt),
-                   dm, gw, dp);
-    // correction at k+1 (waves k, k+1, k+2): its left-neighbour part
-    if (k + 1 <= n - 1)
-      correction_adj(w0, wp1, wp2, dtx, dtx * (mp1.q1 - m0.q1), dtx * (mp1.qn - m0.qn),
-                     dtx * (mp1.qt - m0.qt), gw, dz, dp);
+  const int lane = threadIdx.x & 31;
+  const long long windows = (nx + kWarpCols - 1) / kWarpCols;
+  const long long total = windows * ny;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  const float dtx = dt / p.dx;
+  const float two_bm1 = 2.0f * (p.beta - 1.0f);
+  for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < total; t += nw) {
+    const int win = (int)(t % windows), j = (int)(t / windows);
+    const int i = win * kWarpCols - kHalo + lane;
+    const bool in = i >= 0 && i < nx;
+    const size_t o = in ? size_t(i) + size_t(j) * nx : 0;
+    const Adj3 sa = in ? load_local(s, true, o) : Adj3{0.f, 0.f, 0.f};
+    const Adj3 l = in ? load_local(lo, true, o) : Adj3{0.f, 0.f, 0.f};
+    const Adj3 mu = masked(l, interior(p, i, j));
+    const Adj3 sb = shup(sa), mul = shup(mu);
+    const bool exists = i >= 1 && i <= nx - 1;
+    const WaveN w = sweep_waves(sa, sb, two_bm1, dtx, exists);
+    // the limiter's reverse at interface i
+    WaveAdj cm, c0, cp;
+    zero(cm); zero(c0); zero(cp);
+    {
+      const WaveN wl = shup(w), wr = shdn(w);
+      if (exists)
+        correction_adj(wl, w, wr, dtx, dtx * (mu.q1 - mul.q1), dtx * (mu.qn - mul.qn), dtx * (mu.qt - mul.qt),
+                       cm, c0, cp);
+    }
+    // the waves' adjoint at interface i
+    WaveAdj g = shup(cp);
+    add_to(g, c0);
+    add_to(g, shdn(cm));
     FluctAdj gf;
-    gf.am1 = -dtx * mm1.q1; gf.am2 = -dtx * mm1.qn; gf.am3 = -dtx * mm1.qt;
-    gf.ap1 = -dtx * m0.q1; gf.ap2 = -dtx * m0.qn; gf.ap3 = -dtx * m0.qt;
-    float q1a, qna, qta, q1b, qnb, qtb;
-    local3(s, dir, o, q1a, qna, qta);
-    local3(s, dir, size_t((long long)o - step), q1b, qnb, qtb);
-    riemann_adj(q1a, qna, qta, q1b, qnb, qtb, 2.0f * (p.beta - 1.0f), gw, gf, ga, gb);
+    gf.am1 = -dtx * mul.q1; gf.am2 = -dtx * mul.qn; gf.am3 = -dtx * mul.qt;
+    gf.ap1 = -dtx * mu.q1; gf.ap2 = -dtx * mu.qn; gf.ap3 = -dtx * mu.qt;
+    Adj3 ga{0.f, 0.f, 0.f}, gb{0.f, 0.f, 0.f};
+    if (exists) riemann_adj(sa.q1, sa.qn, sa.qt, sb.q1, sb.qn, sb.qt, two_bm1, g, gf, ga, gb);
+    const Adj3 gbr = shdn(gb);
+    if (in && lane >= kHalo && lane < kLanes - kHalo) {
+      float a1 = 0.f, an = 0.f, at = 0.f;
+      if (i >= 1) { a1 += ga.q1; an += ga.qn; at += ga.qt; }
+      if (i + 1 <= nx - 1) { a1 += gbr.q1; an += gbr.qn; at += gbr.qt; }
+      store_local(li, true, o, Adj3{l.q1 + a1, l.qn + an, l.qt + at});
+    }
   }
-  as.g[0][o] = ga.q1; as.g[1][o] = ga.qn; as.g[2][o] = ga.qt;
-  as.g[3][o] = gb.q1; as.g[4][o] = gb.qn; as.g[5][o] = gb.qt;
 }
 
-// Input adjoint of a sweep: the output adjoint (the update's identity part)
-// plus the cell's share of its two interfaces.
-__global__ void adj_combine_kernel(DevParams p, int dir, CG3 lo, AdjStore as, G3 li) {
-  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+// y sweep: each lane streams one column down a segment of rows [j0, j1),
+// carrying the last three rows' states and adjoints, two interfaces' waves
+// and the limiter reverses' pending parts in registers. Iteration j loads
+// row j, solves interface j, reverses the limiter at j-1 and the solve at
+// j-2, and writes the input adjoint of row j-3.
+__global__ void __launch_bounds__(128) adj_sweep_y_kernel(DevParams p, float dt, CG3 s, CG3 lo, G3 li, int seg) {
   const int nx = p.nx, ny = p.ny;
-  if (i >= nx || j >= ny) return;
-  const size_t o = size_t(i) + size_t(j) * nx;
-  const int k = dir == 0 ? i : j;
-  const int n = dir == 0 ? nx : ny;
-  float a1 = 0.f, an = 0.f, at = 0.f;
-  if (k >= 1) {
-    a1 += as.g[0][o]; an += as.g[1][o]; at += as.g[2][o];
+  const int lane = threadIdx.x & 31;
+  const long long strips = (nx + 31) / 32, nseg = (ny + seg - 1) / seg;
+  const long long total = strips * nseg;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  const float dty = dt / p.dy;
+  const float two_bm1 = 2.0f * (p.beta - 1.0f);
+  for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < total; t += nw) {
+    const int i = (int)(t % strips) * 32 + lane;
+    const int j0 = (int)(t / strips) * seg, j1 = min(ny, j0 + seg);
+    const bool col = i < nx;
+    auto load = [&](int r, Adj3 &sv, Adj3 &lv) {
+      if (col && r >= 0 && r < ny) {
+        const size_t o = size_t(i) + size_t(r) * nx;
+        sv = load_local(s, false, o);
+        lv = load_local(lo, false, o);
+      } else {
+        sv = Adj3{0.f, 0.f, 0.f};
+        lv = Adj3{0.f, 0.f, 0.f};
+      }
+    };
+    Adj3 s1, l1;  // row j-1
+    load(j0 - 3, s1, l1);
+    Adj3 s2{0.f, 0.f, 0.f}, s3{0.f, 0.f, 0.f}, l2{0.f, 0.f, 0.f}, l3{0.f, 0.f, 0.f};  // rows j-2, j-3
+    WaveN w1{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, w2 = w1;  // interfaces j-1, j-2
+    WaveAdj cp1, cp2, c0p;  // cp of the limiter reverses at j-2 and j-3, c0 of the one at j-2
+    zero(cp1); zero(cp2); zero(c0p);
+    Adj3 gap{0.f, 0.f, 0.f};  // ga of the solve at j-3
+    for (int j = j0 - 2; j <= j1 + 2; ++j) {
+      Adj3 s0, l0;
+      load(j, s0, l0);
+      const WaveN w0 = sweep_waves(s0, s1, two_bm1, dty, j >= 1 && j <= ny - 1);
+      const Adj3 mu1 = masked(l1, interior(p, i, j - 1)), mu2 = masked(l2, interior(p, i, j - 2));
+      const Adj3 mu3 = masked(l3, interior(p, i, j - 3));
+      // the limiter's reverse at interface j-1 (waves j-2, j-1, j)
+      WaveAdj cm, c0, cp;
+      zero(cm); zero(c0); zero(cp);
+      if (j - 1 >= 1 && j - 1 <= ny - 1)
+        correction_adj(w2, w1, w0, dty, dty * (mu1.q1 - mu2.q1), dty * (mu1.qn - mu2.qn), dty * (mu1.qt - mu2.qt),
+                       cm, c0, cp);
+      // the waves' adjoint at interface j-2 and the solve's reverse there
+      WaveAdj g = cp2;
+      add_to(g, c0p);
+      add_to(g, cm);
+      FluctAdj gf;
+      gf.am1 = -dty * mu3.q1; gf.am2 = -dty * mu3.qn; gf.am3 = -dty * mu3.qt;
+      gf.ap1 = -dty * mu2.q1; gf.ap2 = -dty * mu2.qn; gf.ap3 = -dty * mu2.qt;
+      Adj3 ga{0.f, 0.f, 0.f}, gb{0.f, 0.f, 0.f};
+      if (j - 2 >= 1 && j - 2 <= ny - 1) riemann_adj(s2.q1, s2.qn, s2.qt, s3.q1, s3.qn, s3.qt, two_bm1, g, gf, ga, gb);
+      // row j-3: lo + ga (solve at j-3) + gb (solve at j-2)
+      const int r3 = j - 3;
+      if (col && r3 >= j0 && r3 < j1) {
+        float a1 = 0.f, an = 0.f, at = 0.f;
+        if (r3 >= 1) { a1 += gap.q1; an += gap.qn; at += gap.qt; }
+        if (r3 + 1 <= ny - 1) { a1 += gb.q1; an += gb.qn; at += gb.qt; }
+        store_local(li, false, size_t(i) + size_t(r3) * nx, Adj3{l3.q1 + a1, l3.qn + an, l3.qt + at});
+      }
+      s3 = s2; s2 = s1; s1 = s0;
+      l3 = l2; l2 = l1; l1 = l0;
+      w2 = w1; w1 = w0;
+      cp2 = cp1; cp1 = cp; c0p = c0;
+      gap = ga;
+    }
   }
-  if (k + 1 <= n - 1) {
-    const size_t q = dir == 0 ? o + 1 : o + size_t(nx);
-    a1 += as.g[3][q]; an += as.g[4][q]; at += as.g[5][q];
-  }
-  li.f[0][o] = lo.f[0][o] + a1;
-  li.f[dir == 0 ? 1 : 2][o] = lo.f[dir == 0 ? 1 : 2][o] + an;
-  li.f[dir == 0 ? 2 : 1][o] = lo.f[dir == 0 ? 2 : 1][o] + at;
 }
 
 __device__ __forceinline__ bool array_row(const DevParams &p, int j) {
@@ -432,8 +491,6 @@ struct fv_adjoint {
   float *stg = nullptr;         // C stage triples (B, S1, S2) of the segment's steps
   float *lam[2][3] = {};        // adjoint ping-pong
   float *tmp[2][3] = {};        // sweep adjoints
-  float *waves[10] = {};
-  float *gab[6] = {};
   float *frame = nullptr;
   float *weights = nullptr;     // amplitudes then phases
   Ctrl *ctrl = nullptr;
@@ -442,6 +499,7 @@ struct fv_adjoint {
   uint32_t *fix = nullptr;
   size_t fix_words = 0;
   int nblocks = 0, fix_blocks = 0, nstrips = 0;
+  int sweep_x_blocks = 0, sweep_y_blocks = 0, sweep_y_seg = 0;  // launch shapes of the reverse sweeps
   float *sched = nullptr;       // dt[nsteps] then T[nsteps]
   double *acc = nullptr;        // loss sum, then gradient sums (2 nelem)
   std::vector<float> h_dt, h_T;
@@ -606,9 +664,9 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   a->dp_replay = a->dp;
   a->dp_replay.cflmax = __builtin_huge_valf();
   // grids: state 2x3, checkpoints, segment (C + 1 states), C stage
-  // triples 3x3, lam 2x3, tmp 2x3, waves 10, gab 6
+  // triples 3x3, lam 2x3, tmp 2x3
   const size_t nstates = 2 + size_t(a->nckpt) + size_t(a->every + 1) + 3 * size_t(a->every) + 2 + 2;
-  const size_t ngrids = nstates * 3 + 10 + 6;
+  const size_t ngrids = nstates * 3;
   cudaError_t e = cudaMalloc(&a->mem, ngrids * a->stride * sizeof(float));
   if (e != cudaSuccess)
     return cleanup(afail(FV_CUDA_ERROR, "cudaMalloc adjoint grids (%zu MB): %s", ngrids * a->stride * 4 >> 20,
@@ -634,9 +692,6 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
     float *base = take(1);
     for (int f = 0; f < 3; ++f) a->tmp[k][f] = base + f * a->stride;
   }
-  for (int k = 0; k < 10; ++k) a->waves[k] = cur + k * a->stride;
-  cur += 10 * a->stride;
-  for (int k = 0; k < 6; ++k) a->gab[k] = cur + k * a->stride;
 
   const int strip_c = kWarpsPerStep * kWarpCols;
   a->nstrips = (p->nx + strip_c - 1) / strip_c;
@@ -645,6 +700,20 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   a->max_resident = per_sm * a->sms;
   a->nblocks = int(std::max(1LL, std::min((long long)a->max_resident, work / 32)));  // one wave
   a->fix_blocks = 4 * a->sms;
+  // reverse sweeps: grid-stride warps, as many CTAs as are resident at once
+  {
+    int ox = 0, oy = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ox, adj_sweep_x_kernel, 128, 0) != cudaSuccess || ox < 1) ox = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oy, adj_sweep_y_kernel, 128, 0) != cudaSuccess || oy < 1) oy = 1;
+    const long long xwarps = (long long)((p->nx + kWarpCols - 1) / kWarpCols) * p->ny;
+    a->sweep_x_blocks = int(std::max(1LL, std::min((long long)ox * a->sms, (xwarps + 3) / 4)));
+    // y sweep: enough row segments to fill the resident warps, at least 16 rows each
+    const long long strips = (p->nx + 31) / 32, ywarps = 4LL * oy * a->sms;
+    const long long nseg = std::max(1LL, std::min((long long)(p->ny + 15) / 16, ywarps / strips));
+    a->sweep_y_seg = int((p->ny + nseg - 1) / nseg);
+    const long long ytotal = strips * ((p->ny + a->sweep_y_seg - 1) / a->sweep_y_seg);
+    a->sweep_y_blocks = int(std::max(1LL, std::min((long long)oy * a->sms, (ytotal + 3) / 4)));
+  }
   a->fix_words = size_t(fix_scratch_words((long long)a->nstrips * kWarpsPerStep, p->ny));
   e = cudaMalloc(&a->frame, 3 * size_t(frame_cells(p->nx, p->ny)) * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&a->weights, 2 * size_t(p->array_elems) * sizeof(float));
@@ -752,10 +821,6 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   if (a->nsteps >= w.step_first && a->nsteps <= w.step_last)
     adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(a->state[a->final_cur][0], a->lam[lc][0], nx, w.i0,
                                                           w.j0, w.ni, w.nj, coef);
-  WaveStore ws;
-  for (int k = 0; k < 10; ++k) ws.w[k] = a->waves[k];
-  AdjStore as;
-  for (int k = 0; k < 6; ++k) as.g[k] = a->gab[k];
   const long long C = a->every;
   for (long long seg0 = ((a->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, a->nsteps);  // steps seg0+1 .. seg1
@@ -790,13 +855,11 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
       // diffusion: lam_n -> tmp0 (adjoint of S2)
       adj_diffusion_kernel<<<grd, blk, 0, a->stream>>>(a->dp, dt, cg3(stage[2]), cg3(lo), g3(a->tmp[0]));
       // x sweep on S1: tmp0 -> tmp1 (adjoint of S1)
-      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(stage[1]), ws);
-      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, dt, cg3(stage[1]), cg3(a->tmp[0]), ws, as);
-      adj_combine_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 0, cg3(a->tmp[0]), as, g3(a->tmp[1]));
+      adj_sweep_x_kernel<<<a->sweep_x_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[1]), cg3(a->tmp[0]),
+                                                                   g3(a->tmp[1]));
       // y sweep on B: tmp1 -> tmp0 (adjoint of B)
-      adj_waves_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(stage[0]), ws);
-      adj_interface_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, dt, cg3(stage[0]), cg3(a->tmp[1]), ws, as);
-      adj_combine_kernel<<<grd, blk, 0, a->stream>>>(a->dp, 1, cg3(a->tmp[1]), as, g3(a->tmp[0]));
+      adj_sweep_y_kernel<<<a->sweep_y_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[0]), cg3(a->tmp[1]),
+                                                                   g3(a->tmp[0]), a->sweep_y_seg);
       // boundary: weights, then lam_{n-1}
       adj_weights_kernel<<<(nelem + 3) / 4, 128, 0, a->stream>>>(a->dp, T, cg3(a->tmp[0]), g_amp, g_ph);
       adj_boundary_kernel<<<grd, blk, 0, a->stream>>>(a->dp, cg3(a->tmp[0]), g3(li));
