@@ -289,7 +289,8 @@ struct fv_handle {
   int snap_cur = -1;            // buffer the snapshot was taken from; -1: none
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;   // kGraphAttempts attempts
+  cudaGraphExec_t graph1 = nullptr;  // fv_run(h, 1): control-block set-up and one attempt
   StepArgs args{};
   int warps = 4;
   bool exact = true;
@@ -446,6 +447,34 @@ void fill_stats(const fv_handle *h, fv_run_stats *st) {
   st->status = c.status;
   st->mdx = c.mdx;
   st->mdy = c.mdy;
+}
+
+// The captured graphs hold the launch shape, division and collector of
+// when they were captured: changing any of them drops them.
+void drop_graphs(fv_handle *h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->graph1) cudaGraphExecDestroy(h->graph1);
+  h->graph = nullptr;
+  h->graph1 = nullptr;
+}
+
+fv_status ensure_graph1(fv_handle *h) {
+  if (h->graph1) return FV_OK;
+  cudaGraph_t g = nullptr;
+  FV_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, 1LL, std::numeric_limits<float>::infinity());
+  int rc = (int)cudaGetLastError();
+  if (rc == 0) rc = launch_attempt(h);
+  cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+  if (rc != 0) return fail(FV_CUDA_ERROR, "step launch during capture: %s", cudaGetErrorString((cudaError_t)rc));
+  if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
+  ec = cudaGraphInstantiate(&h->graph1, g, 0);
+  cudaGraphDestroy(g);
+  if (ec != cudaSuccess) {
+    h->graph1 = nullptr;
+    return fail(FV_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ec));
+  }
+  return FV_OK;
 }
 
 fv_status ensure_graph(fv_handle *h) {
@@ -738,7 +767,7 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
 fv_status fv_destroy(fv_handle *h) {
   if (!h) return FV_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->graph) cudaGraphExecDestroy(h->graph);
+  drop_graphs(h);
   if (h->state_mem) cudaFree(h->state_mem);
   if (h->dbg_mem) cudaFree(h->dbg_mem);
   if (h->frame_mem) cudaFree(h->frame_mem);
@@ -867,10 +896,7 @@ fv_status fv_render(fv_handle *h, const fv_render_spec *spec, uint8_t *rgba, int
 fv_status fv_collect_enable(fv_handle *h, const fv_collect_spec *spec) {
   if (!h) return fail(FV_BAD_ARG, "handle is NULL");
   FV_CUDA(cudaStreamSynchronize(h->stream));
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
+  drop_graphs(h);
   if (h->coll_mem) cudaFree(h->coll_mem);
   h->coll_mem = nullptr;
   h->collect = false;
@@ -1059,12 +1085,21 @@ fv_status fv_sync(fv_handle *h, fv_run_stats *out) {
 
 fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
   if (!h || nsteps < 0) return fail(FV_BAD_ARG, "bad argument");
-  ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nsteps,
-                                            std::numeric_limits<float>::infinity());
-  FV_CUDA(cudaGetLastError());
   long long todo = nsteps;
+  if (nsteps == 1) {
+    // one step, the call of a caller that reads every step's stats: the
+    // control-block set-up and the attempt as one graph launch
+    fv_status s = ensure_graph1(h);
+    if (s != FV_OK) return s;
+    FV_CUDA(cudaGraphLaunch(h->graph1, h->stream));
+    todo = 0;
+  } else {
+    ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nsteps,
+                                              std::numeric_limits<float>::infinity());
+    FV_CUDA(cudaGetLastError());
+  }
   for (;;) {
-    fv_status s = enqueue_attempts(h, todo);
+    fv_status s = todo > 0 ? enqueue_attempts(h, todo) : FV_OK;
     if (s != FV_OK) return s;
     s = read_ctrl(h);
     if (s != FV_OK) return s;
@@ -1107,10 +1142,7 @@ fv_status fv_set_launch(fv_handle *h, int32_t blocks) {
   if (b > h->partials_cap) return fail(FV_BAD_ARG, "blocks %lld above %d", b, h->partials_cap);
   FV_CUDA(cudaStreamSynchronize(h->stream));
   h->args.nblocks = int(b);
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
+  drop_graphs(h);
   return FV_OK;
 }
 
@@ -1125,10 +1157,7 @@ fv_status fv_set_division(fv_handle *h, int32_t mode) {
   if (!h || mode < FV_DIVISION_DEFAULT || mode > FV_DIVISION_EXACT) return fail(FV_BAD_ARG, "bad argument");
   FV_CUDA(cudaStreamSynchronize(h->stream));
   h->args.div_exact = mode == FV_DIVISION_DEFAULT ? default_div_exact(h->params) : (mode == FV_DIVISION_EXACT);
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
+  drop_graphs(h);
   return FV_OK;
 }
 
