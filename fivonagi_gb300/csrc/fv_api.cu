@@ -416,7 +416,6 @@ void init_host(const fv_params &p, const DevParams &d, float *u1, float *u2, flo
 
 namespace fvgb {
 DevParams dev_params_of(const fv_params &p) { return make_dev_params(p); }
-int strip_cols() { return 4 * kWarpCols; }
 fv_status validate_params(const fv_params *p) { return validate(p); }
 void init_state_host(const fv_params &p, float *u1, float *u2, float *u3) {
   init_host(p, make_dev_params(p), u1, u2, u3);

@@ -205,13 +205,12 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
     const size_t fc = (size_t(frame_cells(params[k].nx, params[k].ny)) + 63) & ~size_t(63);
     for (int f = 0; f < 3; ++f) I.frame[f] = b->mem + off_frame[k] + size_t(f) * fc;
     I.ctrl = b->ctrl + k;
-    const int nstrips = (params[k].nx + strip_cols() - 1) / strip_cols();
     const int windows = (params[k].nx + kWarpCols - 1) / kWarpCols;
     I.work_begin = work;
     I.work = (long long)windows * params[k].ny;
     work += I.work;
     I.fix_base = fix_chunks;
-    fix_chunks += (long long)nstrips * (strip_cols() / kWarpCols) * fix_chunks_per_window(params[k].ny);
+    fix_chunks += (long long)windows * fix_chunks_per_window(params[k].ny);
     max_frame = std::max(max_frame, 4 * params[k].nx + 4 * (params[k].ny - 4));
   }
   if (fix_chunks >= (1LL << 32)) return cleanup(bfail(FV_BAD_ARG, "batch above 2^32 fix-up chunks"));

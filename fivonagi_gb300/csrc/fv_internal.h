@@ -170,6 +170,5 @@ DevParams dev_params_of(const fv_params &p);
 fv_status validate_params(const fv_params *p);
 void init_state_host(const fv_params &p, float *u1, float *u2, float *u3);
 void set_last_error(const char *msg);
-int strip_cols();  // output columns per strip of the step kernel
 
 }  // namespace fvgb
