@@ -13,9 +13,8 @@
 // of u1^2 over a window of cells and a range of accepted steps.
 //
 // Forward: the ordinary attempt launches (ghost frame, step, fix-up,
-// finalize), with
-// three one-thread kernels around each attempt that record the dt and T of
-// accepted steps, copy a checkpoint every C accepted steps and add the
+// finalize), each followed by one record launch that keeps the dt and T of
+// accepted steps, copies a checkpoint every C accepted steps and adds the
 // step's window sum to the loss -- all device-side, no host round trip per
 // step. Backward: segment by segment from the last checkpoint, replay the
 // segment's steps from its checkpoint (frozen dt) into a buffer of C
@@ -89,35 +88,10 @@ __global__ void adj_pre_kernel(const Ctrl *c, AdjRec *r) {
   r->accepted = 0;
 }
 
-__global__ void adj_post_kernel(const Ctrl *c, AdjRec *r, float *sched_dt, float *sched_T, int nsteps) {
-  if (c->n == r->n0 + 1 && r->n0 < nsteps) {
-    r->accepted = 1;
-    sched_dt[r->n0] = r->dt0;
-    sched_T[r->n0] = r->T0;
-  }
-}
-
-// After an accepted attempt: the checkpoint every `every` steps.
-__global__ void adj_checkpoint_kernel(const Ctrl *c, const AdjRec *r, G3 s0, G3 s1, float *ckpt,
-                                      size_t stride, size_t ncell, int every) {
-  if (!r->accepted) return;
-  const int n = c->n;
-  if (n % every != 0) return;
-  const G3 &src = c->cur ? s1 : s0;
-  float *dst = ckpt + size_t(n / every) * 3 * stride;
-  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < ncell; k += size_t(gridDim.x) * blockDim.x) {
-    dst[k] = src.f[0][k];
-    dst[stride + k] = src.f[1][k];
-    dst[2 * stride + k] = src.f[2][k];
-  }
-}
-
-// Window sum of u1^2 of the current state after an accepted attempt whose
-// step lies in [first, last]; `rec` may be null (replays: every attempt is
-// accepted).
-__global__ void adj_loss_kernel(const Ctrl *c, const AdjRec *r, G3 s0, G3 s1, int nx, int i0, int j0,
-                                int ni, int nj, long long first, long long last, double *acc) {
-  if (r && !r->accepted) return;
+// Window sum of u1^2 of the current state after a replayed attempt (every
+// replayed attempt is accepted) whose step lies in [first, last].
+__global__ void adj_loss_kernel(const Ctrl *c, G3 s0, G3 s1, int nx, int i0, int j0, int ni, int nj,
+                                long long first, long long last, double *acc) {
   const long long n = c->n;
   if (n < first || n > last) return;
   const float *u1 = (c->cur ? s1 : s0).f[0];
@@ -135,6 +109,61 @@ __global__ void adj_loss_kernel(const Ctrl *c, const AdjRec *r, G3 s0, G3 s1, in
     __syncthreads();
   }
   if (threadIdx.x == 0) atomicAdd(acc, red[0]);
+}
+
+// After attempt k of the recorded forward, whose scalars before the attempt
+// are in rec[parity] (parity = k & 1): whether it was accepted (n advanced
+// by one); then its dt and T into the schedule, the checkpoint every
+// `every` steps (all blocks) and the window sum of u1^2 (block 0), and the
+// scalars before attempt k+1 into rec[parity ^ 1]. One launch per attempt
+// instead of a snapshot, a record, a checkpoint and a loss launch; the two
+// slots keep block 0's write of the next snapshot from racing with the
+// other blocks' read of this one.
+__global__ void adj_record_kernel(const Ctrl *c, AdjRec *rec, int parity, float *sched_dt, float *sched_T,
+                                  int nsteps, G3 s0, G3 s1, float *ckpt, size_t stride, size_t ncell, int every,
+                                  int nx, int i0, int j0, int ni, int nj, long long first, long long last,
+                                  double *acc) {
+  const AdjRec r = rec[parity];
+  const int n = c->n;
+  const bool accepted = (n == r.n0 + 1) && r.n0 < nsteps;
+  const G3 &src = c->cur ? s1 : s0;
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) {
+      if (accepted) {
+        sched_dt[r.n0] = r.dt0;
+        sched_T[r.n0] = r.T0;
+      }
+      AdjRec &next = rec[parity ^ 1];
+      next.dt0 = c->dt;
+      next.T0 = c->T;
+      next.n0 = n;
+      next.accepted = 0;
+    }
+    if (accepted && n >= first && n <= last) {
+      double sum = 0.0;
+      for (int k = threadIdx.x; k < ni * nj; k += blockDim.x) {
+        const int i = i0 + k % ni, j = j0 + k / ni;
+        const double v = src.f[0][i + size_t(j) * nx];
+        sum += v * v;
+      }
+      __shared__ double red[256];
+      red[threadIdx.x] = sum;
+      __syncthreads();
+      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) atomicAdd(acc, red[0]);
+    }
+  }
+  if (accepted && n % every == 0) {
+    float *dst = ckpt + size_t(n / every) * 3 * stride;
+    for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < ncell; k += size_t(gridDim.x) * blockDim.x) {
+      dst[k] = src.f[0][k];
+      dst[stride + k] = src.f[1][k];
+      dst[2 * stride + k] = src.f[2][k];
+    }
+  }
 }
 
 // Scalars of step n of the frozen schedule (0-based: the step from u_n).
@@ -569,16 +598,16 @@ fv_status run_forward(fv_adjoint *a, bool record, double *loss) {
     const StepArgs s = step_args(a, a->dp, a->state[0], a->state[1]);
     const int cgrid = std::max(1, a->sms * 4);
     long long todo = a->nsteps;
+    long long attempt = 0;
+    adj_pre_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->rec);  // the scalars before attempt 0
     for (int round = 0; round < 64 && todo > 0; ++round) {
-      for (long long k = 0; k < todo; ++k) {
-        adj_pre_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->rec);
+      for (long long k = 0; k < todo; ++k, ++attempt) {
         int rc = launch(a, s, -1);
         if (rc != 0) return afail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
-        adj_post_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->rec, a->sched, a->sched + a->nsteps, int(a->nsteps));
-        adj_checkpoint_kernel<<<cgrid, 256, 0, a->stream>>>(a->ctrl, a->rec, s0, s1, a->ckpt, a->stride, a->ncell,
-                                                             a->every);
-        adj_loss_kernel<<<1, 256, 0, a->stream>>>(a->ctrl, a->rec, s0, s1, P.nx, w.i0, w.j0, w.ni, w.nj,
-                                                   w.step_first, w.step_last, a->acc);
+        adj_record_kernel<<<cgrid, 256, 0, a->stream>>>(a->ctrl, a->rec, int(attempt & 1), a->sched,
+                                                         a->sched + a->nsteps, int(a->nsteps), s0, s1, a->ckpt,
+                                                         a->stride, a->ncell, a->every, P.nx, w.i0, w.j0, w.ni,
+                                                         w.nj, w.step_first, w.step_last, a->acc);
       }
       FVA_CUDA(cudaGetLastError());
       Ctrl c;
@@ -599,7 +628,7 @@ fv_status run_forward(fv_adjoint *a, bool record, double *loss) {
       adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n), -1);
       int rc = launch(a, s, -1);
       if (rc != 0) return afail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
-      adj_loss_kernel<<<1, 256, 0, a->stream>>>(a->ctrl, nullptr, s0, s1, P.nx, w.i0, w.j0, w.ni, w.nj,
+      adj_loss_kernel<<<1, 256, 0, a->stream>>>(a->ctrl, s0, s1, P.nx, w.i0, w.j0, w.ni, w.nj,
                                                  w.step_first, w.step_last, a->acc);
     }
     FVA_CUDA(cudaGetLastError());
@@ -718,7 +747,7 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   e = cudaMalloc(&a->frame, 3 * size_t(frame_cells(p->nx, p->ny)) * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&a->weights, 2 * size_t(p->array_elems) * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&a->ctrl, sizeof(Ctrl));
-  if (e == cudaSuccess) e = cudaMalloc(&a->rec, sizeof(AdjRec));
+  if (e == cudaSuccess) e = cudaMalloc(&a->rec, 2 * sizeof(AdjRec));  // two slots, by attempt parity
   if (e == cudaSuccess) e = cudaMalloc(&a->partials, size_t(a->nblocks + a->fix_blocks) * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&a->fix, a->fix_words * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&a->sched, 2 * size_t(nsteps) * sizeof(float));
