@@ -21,9 +21,10 @@
 // states; each replayed attempt also records its stage grids B, Y, X (the
 // step kernel writes them as it goes, kStageRecord), the linearisation
 // points of the reverse step. Then walk the segment backwards. A reverse
-// step runs the reverse kernels: diffusion; one fused kernel per sweep
-// (waves, limiter reverse, solve reverse and the per-cell gather, with the
-// sweep's neighbours in registers and warp shuffles); boundary (ghost cells
+// step runs the reverse kernels: one fused kernel per sweep (waves,
+// limiter reverse, solve reverse and the per-cell gather, with the sweep's
+// neighbours in registers and warp shuffles; the x sweep's kernel also
+// reverses the diffusion); boundary (ghost cells
 // back to the cells they copy, and the source cells to the weights).
 // Memory: 3 (N / C) + 12 C + ~21 grids; C = ceil(sqrt(N)) by default.
 #include <cuda_runtime.h>
@@ -204,38 +205,6 @@ __global__ void adj_ctrl_reset_kernel(Ctrl *c, float dt, float T, long long rema
 
 // ------------------------------------------------------------ reverse kernels
 
-// Diffusion (source, apps/na/source.h:22-104): o1 = (u1 + 1) - 1,
-// o2 = u2 + ddtx2 (vx(i-1) - 2 vx + vx(i+1)) + ddty2 (vx(j-1) - 2 vx + vx(j+1)),
-// o3 likewise with vy, on interior cells; identity elsewhere.
-__global__ void adj_diffusion_kernel(DevParams p, float dt, CG3 s2, CG3 lo, G3 li) {
-  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
-  const int nx = p.nx, ny = p.ny;
-  if (i >= nx || j >= ny) return;
-  const size_t o = size_t(i) + size_t(j) * nx;
-  const float ddtx2 = p.diffdelta * dt / (p.dx * p.dx);
-  const float ddty2 = p.diffdelta * dt / (p.dy * p.dy);
-  float gvx = 0.f, gvy = 0.f;
-  if (interior(p, i, j)) {
-    gvx -= 2.0f * (ddtx2 + ddty2) * lo.f[1][o];
-    gvy -= 2.0f * (ddtx2 + ddty2) * lo.f[2][o];
-  }
-  const int ni[4] = {i - 1, i + 1, i, i};
-  const int nj[4] = {j, j, j - 1, j + 1};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (!interior(p, ni[k], nj[k])) continue;
-    const size_t q = size_t(ni[k]) + size_t(nj[k]) * nx;
-    const float c = k < 2 ? ddtx2 : ddty2;
-    gvx += c * lo.f[1][q];
-    gvy += c * lo.f[2][q];
-  }
-  const float rho = s2.f[0][o] + 1.0f;
-  const float vx = fdiv(s2.f[1][o], rho), vy = fdiv(s2.f[2][o], rho);
-  li.f[0][o] = lo.f[0][o] - fdiv(gvx * vx + gvy * vy, rho);
-  li.f[1][o] = lo.f[1][o] + fdiv(gvx, rho);
-  li.f[2][o] = lo.f[2][o] + fdiv(gvy, rho);
-}
-
 // Local frame of a sweep: component 1 = u1; x sweep: normal = u2,
 // transverse = u3; y sweep: normal = u3, transverse = u2
 // (apps/na/fv.h:489-493).
@@ -309,7 +278,43 @@ __device__ __forceinline__ Adj3 masked(const Adj3 &v, bool keep) {
 // halo each side (the columns of the step kernel's windows); neighbours are
 // neighbouring lanes. A warp takes (window, row) pairs, consecutive warps
 // neighbouring windows of one row.
-__global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt, CG3 s, CG3 lo, G3 li) {
+//
+// The x sweep's kernel also reverses the diffusion that follows the sweep
+// (source, apps/na/source.h:22-104): o1 = (u1 + 1) - 1, o2 = u2 +
+// ddtx2 (vx(i-1) - 2 vx + vx(i+1)) + ddty2 (vx(j-1) - 2 vx + vx(j+1)), o3
+// likewise with vy, on interior cells, identity elsewhere; v = u / rho of
+// the x-swept state s2. From the output adjoint lam it forms the sweep's
+// output adjoint lo at each lane's cell (the neighbours along the row are
+// neighbouring lanes), so lo never passes through memory.
+__device__ __forceinline__ Adj3 diffusion_reverse(const DevParams &p, float ddtx2, float ddty2, int i, int j,
+                                                  bool in, size_t o, const CG3 &s2, const CG3 &lam) {
+  const int nx = p.nx, ny = p.ny;
+  float l0 = 0.f, l1 = 0.f, l2 = 0.f;  // lam at (i, j), global components
+  float d1 = 0.f, d2 = 0.f, u1 = 0.f, u2 = 0.f;  // lam components 2, 3 at (i, j-1), (i, j+1)
+  float q0 = 0.f, q1 = 0.f, q2 = 0.f;  // s2 at (i, j)
+  if (in) {
+    l0 = lam.f[0][o]; l1 = lam.f[1][o]; l2 = lam.f[2][o];
+    q0 = s2.f[0][o]; q1 = s2.f[1][o]; q2 = s2.f[2][o];
+    if (j - 1 >= 0) { d1 = lam.f[1][o - nx]; d2 = lam.f[2][o - nx]; }
+    if (j + 1 < ny) { u1 = lam.f[1][o + nx]; u2 = lam.f[2][o + nx]; }
+  }
+  const float lm1 = shup(l1), lm2 = shup(l2), lp1 = shdn(l1), lp2 = shdn(l2);
+  float gvx = 0.f, gvy = 0.f;
+  if (interior(p, i, j)) {
+    gvx -= 2.0f * (ddtx2 + ddty2) * l1;
+    gvy -= 2.0f * (ddtx2 + ddty2) * l2;
+  }
+  if (interior(p, i - 1, j)) { gvx += ddtx2 * lm1; gvy += ddtx2 * lm2; }
+  if (interior(p, i + 1, j)) { gvx += ddtx2 * lp1; gvy += ddtx2 * lp2; }
+  if (interior(p, i, j - 1)) { gvx += ddty2 * d1; gvy += ddty2 * d2; }
+  if (interior(p, i, j + 1)) { gvx += ddty2 * u1; gvy += ddty2 * u2; }
+  const float rho = q0 + 1.0f;
+  const float vx = fdiv(q1, rho), vy = fdiv(q2, rho);
+  // local frame of the x sweep: q1 = u1, qn = u2, qt = u3
+  return Adj3{l0 - fdiv(gvx * vx + gvy * vy, rho), l1 + fdiv(gvx, rho), l2 + fdiv(gvy, rho)};
+}
+
+__global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt, CG3 s, CG3 s2, CG3 lam, G3 li) {
   const int nx = p.nx, ny = p.ny;
   const int lane = threadIdx.x & 31;
   const long long windows = (nx + kWarpCols - 1) / kWarpCols;
@@ -317,13 +322,15 @@ __global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt,
   const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
   const float dtx = dt / p.dx;
   const float two_bm1 = 2.0f * (p.beta - 1.0f);
+  const float ddtx2 = p.diffdelta * dt / (p.dx * p.dx);
+  const float ddty2 = p.diffdelta * dt / (p.dy * p.dy);
   for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < total; t += nw) {
     const int win = (int)(t % windows), j = (int)(t / windows);
     const int i = win * kWarpCols - kHalo + lane;
     const bool in = i >= 0 && i < nx;
     const size_t o = in ? size_t(i) + size_t(j) * nx : 0;
     const Adj3 sa = in ? load_local(s, true, o) : Adj3{0.f, 0.f, 0.f};
-    const Adj3 l = in ? load_local(lo, true, o) : Adj3{0.f, 0.f, 0.f};
+    const Adj3 l = diffusion_reverse(p, ddtx2, ddty2, i, j, in, o, s2, lam);
     const Adj3 mu = masked(l, interior(p, i, j));
     const Adj3 sb = shup(sa), mul = shup(mu);
     const bool exists = i >= 1 && i <= nx - 1;
@@ -881,11 +888,9 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
         for (int f = 0; f < 3; ++f) stage[st][f] = stage_grid(a, n - 1 - seg0, st, f);
       float *const *lo = a->lam[lc];
       float *const *li = a->lam[lc ^ 1];
-      // diffusion: lam_n -> tmp0 (adjoint of S2)
-      adj_diffusion_kernel<<<grd, blk, 0, a->stream>>>(a->dp, dt, cg3(stage[2]), cg3(lo), g3(a->tmp[0]));
-      // x sweep on S1: tmp0 -> tmp1 (adjoint of S1)
-      adj_sweep_x_kernel<<<a->sweep_x_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[1]), cg3(a->tmp[0]),
-                                                                   g3(a->tmp[1]));
+      // diffusion (on S2) and x sweep (on S1): lam_n -> tmp1 (adjoint of S1)
+      adj_sweep_x_kernel<<<a->sweep_x_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[1]), cg3(stage[2]),
+                                                                   cg3(lo), g3(a->tmp[1]));
       // y sweep on B: tmp1 -> tmp0 (adjoint of B)
       adj_sweep_y_kernel<<<a->sweep_y_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[0]), cg3(a->tmp[1]),
                                                                    g3(a->tmp[0]), a->sweep_y_seg);
