@@ -244,27 +244,29 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     XOut xo;
     auto y_chain = [&](auto &dp) {
       const float rho = u.u1 + 1.0f;
-      const auto rr = dp.recip(rho);
-      yo.vx = dp.div_r(u.u2, rr);
-      yo.vy = dp.div_r(u.u3, rr);
+      const auto rr = dp.s.recip(rho);
+      yo.vx = dp.s.div_r(u.u2, rr);
+      yo.vy = dp.x.div_r(u.u3, rr);
       yo.cy = 0.0f;
-      yo.ok = riemann(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
-                      vx_m1, two_bm1, dty, yo.cy, yo.w, yo.f, dp);
+      // normal = u3: the normal velocity's quotients are the others (DivPair)
+      yo.ok = riemann<true>(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
+                            vx_m1, two_bm1, dty, yo.cy, yo.w, yo.f, dp.s, dp.x);
       yo.dr = wave_dots(w_m1, yo.w);
-      correction(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp);
+      correction(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp.s);
     };
     auto x_chain = [&](auto &dp) {
       const float rho1 = s1_m3.u1 + 1.0f;
-      const auto rr = dp.recip(rho1);
-      const float vn1 = dp.div_r(s1_m3.u2, rr);
-      const float vt1 = dp.div_r(s1_m3.u3, rr);
+      const auto rr = dp.s.recip(rho1);
+      const float vn1 = dp.s.div_r(s1_m3.u2, rr);
+      const float vt1 = dp.x.div_r(s1_m3.u3, rr);
       const float rho1m = shup(rho1), u2m = shup(s1_m3.u2), u3m = shup(s1_m3.u3);
       const float vn1m = shup(vn1), vt1m = shup(vt1);
       WaveN wx;
       Fluct fx;
       xo.cx = cy_m3;  // the x kernel starts from the cell's y value (fv.h:57)
-      xo.ok = riemann(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m, two_bm1,
-                      dtx, xo.cx, wx, fx, dp);
+      // transverse = u3: the transverse velocity's quotients are the others
+      xo.ok = riemann<false>(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m, two_bm1,
+                             dtx, xo.cx, wx, fx, dp.s, dp.x);
       WaveN wn;
       wn.w11 = shdn(wx.w11); wn.w21 = shdn(wx.w21); wn.w31 = shdn(wx.w31);
       wn.w12 = shdn(wx.w12); wn.w22 = shdn(wx.w22); wn.w32 = shdn(wx.w32);
@@ -273,7 +275,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       Dots dlx;
       dlx.d1 = shup(drx.d1); dlx.d2 = shup(drx.d2); dlx.d3 = shup(drx.d3);
       float fx1, fx2, fx3;
-      correction(wx, dlx, drx, dtx, fx1, fx2, fx3, dp);
+      correction(wx, dlx, drx, dtx, fx1, fx2, fx3, dp.s);
       const float amn1 = shdn(fx.am1), amn2 = shdn(fx.am2), amn3 = shdn(fx.am3);
       const float fxn1 = shdn(fx1), fxn2 = shdn(fx2), fxn3 = shdn(fx3);
       const bool in_x = col_int && r - 3 >= 2 && r - 3 <= ny - 3;
@@ -284,9 +286,9 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       xo.s2.u2 = in_x ? m2 - dtx * (fxn2 - fx2) : s1_m3.u2;
       xo.s2.u3 = in_x ? m3 - dtx * (fxn3 - fx3) : s1_m3.u3;
       const float rho2 = xo.s2.u1 + 1.0f;
-      const auto rr2 = dp.recip(rho2);
-      xo.vx2 = dp.div_r(xo.s2.u2, rr2);
-      xo.vy2 = dp.div_r(xo.s2.u3, rr2);
+      const auto rr2 = dp.s.recip(rho2);
+      xo.vx2 = dp.s.div_r(xo.s2.u2, rr2);
+      xo.vy2 = dp.x.div_r(xo.s2.u3, rr2);
     };
     DP dy, dx;
     if constexpr (RY) y_chain(dy);
@@ -573,13 +575,14 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     for (int f = 0; f < 3; ++f) out[f] = (STAGE < 0) ? a.state[cur ^ 1][f] : a.dbg[f];
   }
   const float *frame[3] = {a.frame[0], a.frame[1], a.frame[2]};
-  // Exact division (DivExact) for kStageExactDiv and for the adjoint's
-  // stage-recording replays: the fix-up pass then has no work. It costs
-  // the step kernel 2-5% more than FMA division; whether the fix-up pass it
-  // saves is worth more depends on the grid (see fv_set_division). The
-  // replays gain 3% per backward step at 1024x1024.
-  using DP = typename std::conditional<(STAGE == kStageRecord || STAGE == kStageExactDiv), DivExact,
-                                       typename std::conditional<(STAGE < 0), DivFma, DivIEEE>::type>::type;
+  // Exact division for kStageExactDiv and for the adjoint's
+  // stage-recording replays (DivNormal where quotients are normal in
+  // practice, DivExact where they can be subnormal): the fix-up pass then
+  // has no work in practice. Whether that beats FMA division with its
+  // fix-up pass depends on the grid (see fv_set_division). The replays
+  // gain 3% per backward step at 1024x1024.
+  using DP = typename std::conditional<(STAGE == kStageRecord || STAGE == kStageExactDiv), PairNormalExact,
+                                       typename std::conditional<(STAGE < 0), PairFma, PairIEEE>::type>::type;
 
   const int warp = threadIdx.x >> 5;
   const int ny = a.p.ny;
@@ -668,13 +671,13 @@ __global__ void __launch_bounds__(kThreads, 2) fixup_kernel(StepArgs a) {
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<STAGE, DivExact, kFixPrefetch>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm,
-                                                 ng, fm);
+    stream_window<STAGE, PairExact, kFixPrefetch>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm,
+                                                  ng, fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
       NoMarker none;
-      stream_window<STAGE, DivIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+      stream_window<STAGE, PairIEEE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
     }
     cmax = nanmax(cmax, cm);
     neg = neg || ng;
@@ -830,8 +833,8 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
         const long long left = seg_end - q;
         const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
         BatchMarker mk{b, k, -1};
-        stream_window<-1, DivFma>(p, in, frame, out, win * kWarpCols, y0, y1, dt, T, mdx, mdy, shx, shy, cmax,
-                                  neg, mk);
+        stream_window<-1, PairFma>(p, in, frame, out, win * kWarpCols, y0, y1, dt, T, mdx, mdy, shx, shy, cmax,
+                                   neg, mk);
         q += y1 - y0;
       }
       for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
@@ -885,12 +888,12 @@ __global__ void __launch_bounds__(kThreads, 2) batch_fixup_kernel(BatchArgs b) {
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<-1, DivExact, kFixPrefetch>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    stream_window<-1, PairExact, kFixPrefetch>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
       NoMarker none;
-      stream_window<-1, DivIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+      stream_window<-1, PairIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
     }
     for (int off = 16; off > 0; off >>= 1) cm = nanmax(cm, __shfl_xor_sync(0xffffffffu, cm, off));
     const bool wneg = __any_sync(0xffffffffu, ng);

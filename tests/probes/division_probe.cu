@@ -13,6 +13,7 @@
 //  3. Sampled DivExact::div() over the same classes, and DivExact::ratio()
 //     over the limiter's: every quotient it does not flag (it flags only
 //     operands out of range, NaN and infinity) must equal the IEEE quotient.
+//     The same for DivNormal::div(), which also flags subnormal quotients.
 //  4. Sampled ratio(): the limiter's quotient of a product-like dividend
 //     and a positive sum-of-squares divisor. Unflagged results equal the
 //     IEEE quotient, or, where that exceeds 2^59 in magnitude, have its sign
@@ -139,6 +140,33 @@ __global__ void exact_sample(int mode, uint64_t seed, long long n, unsigned long
   if (bd) atomicAdd(bad, bd);
 }
 
+// DivNormal (the exact-division step kernel's policy for quotients that are
+// normal in practice): every quotient it does not flag equals IEEE division
+__global__ void normal_sample(int mode, uint64_t seed, long long n, unsigned long long *flagged,
+                              unsigned long long *bad, float *example) {
+  unsigned long long fl = 0, bd = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    float a, b;
+    operands(mode, mix(seed + 2 * (uint64_t)k), mix(seed + 2 * (uint64_t)k + 1), a, b);
+    fvgb::DivNormal d;
+    const float q = d.div(a, b);
+    if (d.unsafe()) {
+      ++fl;
+      continue;
+    }
+    const float ref = a / b;
+    if (__float_as_uint(q) != __float_as_uint(ref) && !(q != q && ref != ref)) {
+      ++bd;
+      example[0] = a;
+      example[1] = b;
+      example[2] = q;
+    }
+  }
+  if (fl) atomicAdd(flagged, fl);
+  if (bd) atomicAdd(bad, bd);
+}
+
 // the limiter's operands: a = sum of products of wave components, b = sum
 // of their squares (> 0); exponents anywhere from subnormal to large
 __global__ void ratio_sample(int mode, uint64_t seed, long long n, unsigned long long *flagged,
@@ -234,6 +262,18 @@ int main(int argc, char **argv) {
     cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
     cudaMemcpy(e, ex, 3 * sizeof(float), cudaMemcpyDeviceToHost);
     std::printf("xdiv_%s %lld %llu %llu", names[mode], per_mode / 4, h[0], h[1]);
+    if (h[1]) std::printf("  a=%a b=%a got=%a", e[0], e[1], e[2]);
+    std::printf("\n");
+    if (h[1]) rc = 1;
+  }
+  // 3b. the exact-division step kernel's normal-quotient division
+  for (int mode = 0; mode < 14; ++mode) {
+    cudaMemset(cnt, 0, 2 * sizeof(unsigned long long));
+    normal_sample<<<grid, 256>>>(mode, 0x90a10000ull + 7919ull * mode, per_mode / 4, cnt, cnt + 1, ex);
+    float e[4] = {0, 0, 0, 0};
+    cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaMemcpy(e, ex, 3 * sizeof(float), cudaMemcpyDeviceToHost);
+    std::printf("ndiv_%s %lld %llu %llu", names[mode], per_mode / 4, h[0], h[1]);
     if (h[1]) std::printf("  a=%a b=%a got=%a", e[0], e[1], e[2]);
     std::printf("\n");
     if (h[1]) rc = 1;

@@ -54,6 +54,11 @@ def test_fma_division_is_ieee_where_not_flagged(tmp_path):
     # flags nothing in the classes the solver produces, tiny and subnormal
     # dividends included
     assert sum(1 for k in rows if k.startswith("xdiv_")) == 14
+    # the normal-quotient division: checked on every class (bad == 0 above);
+    # it flags nothing where the solver's quotients are normal
+    assert sum(1 for k in rows if k.startswith("ndiv_")) == 14
+    for name in ("solver_like", "dividend_2^-100", "exact_quotients"):
+        assert rows["ndiv_" + name][1] == 0, rows["ndiv_" + name][3]
     for name in ("solver_like", "tiny_dividend", "subnormal_dividend",
                  "dividend_2^-100", "tail_divisors", "exact_quotients"):
         assert rows["xdiv_" + name][1] == 0, rows["xdiv_" + name][3]
