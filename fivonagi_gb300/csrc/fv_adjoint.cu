@@ -563,6 +563,7 @@ StepArgs step_args(const fv_adjoint *a, const DevParams &dp, float *const in[3],
   s.nblocks = a->nblocks;
   s.work = (long long)a->nstrips * a->params.ny;
   s.fix_blocks = a->fix_blocks;
+  s.div_exact = 1;  // exact division in the step kernel, as fv_create's default
   return s;
 }
 

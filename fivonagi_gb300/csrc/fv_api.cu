@@ -516,12 +516,13 @@ fv_status enqueue_attempts(fv_handle *h, long long n) {
 // of rows, so all CTAs of a wave finish together; a second wave would add
 // the warm-up rows of shorter segments, and a partial one (for instance 640
 // CTAs for 608 slots) nearly doubles the time.
-// Exact division in the step kernel from 2^21 cells up. It costs the step
-// kernel 2-5% over FMA division and saves the fix-up pass (about 30 us,
-// nearly independent of the grid): measured per attempt, 0.503 against
-// 0.527 ms at 4096x2048 and 0.168 against 0.177 ms at 2048x1024, but 0.111
-// against 0.106 ms at 1024x1024, where the state stays in L2.
-int default_div_exact(const fv_params &p) { return (long long)p.nx * p.ny >= (1LL << 21) ? 1 : 0; }
+// Exact division in the step kernel by default. With the normal-quotient
+// division where quotients are normal in practice (DivPair), it is faster
+// than FMA division with its fix-up pass at every size measured: per
+// attempt 0.056 against 0.061 ms at 512x512, 0.096 against 0.109 ms at
+// 1024x1024, 0.144 against 0.165 ms at 2048x1024, 0.447 against 0.498 ms
+// at 4096x2048.
+int default_div_exact(const fv_params &) { return 1; }
 
 long long default_blocks(int max_resident, long long work) {
   return std::max(1LL, std::min((long long)max_resident, work / kMinRowsPerBlock));

@@ -297,9 +297,10 @@ fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident);
  *   FV_DIVISION_FMA: FMA-based division, with a fix-up pass that recomputes
  *     the few rows where its operands leave its proven range (subnormal
  *     quotients) with exact division;
- *   FV_DIVISION_EXACT: exact division in the step kernel itself, slower per
- *     row, with no fix-up work;
- *   FV_DIVISION_DEFAULT: EXACT from 2^21 cells up, FMA below.
+ *   FV_DIVISION_EXACT: exact division in the step kernel itself (the
+ *     subnormal-proof form only for the quotients that can be subnormal),
+ *     with no fix-up work in practice;
+ *   FV_DIVISION_DEFAULT: EXACT (the faster at every size measured).
  * No reference counterpart: the reference uses the compiler's division. */
 #define FV_DIVISION_DEFAULT (-1)
 #define FV_DIVISION_FMA 0

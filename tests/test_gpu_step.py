@@ -302,8 +302,10 @@ def test_timed_attempts_match_ordinary_attempts(blocks, division):
 @pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (0, 130, 300), (1, 104, 64), (4, 96, 64)])
 def test_division_modes_give_the_same_results(app, nx, ny):
     """FMA division with its fix-up pass and exact division in the step
-    kernel both give IEEE quotients: the runs agree bit for bit (the FMA
-    mode is the one the oracle parity tests run on small grids)."""
+    kernel both give IEEE quotients: the runs agree bit for bit. The oracle
+    parity tests run the default (exact) division, so FMA division matches
+    the oracle as well, and its fix-up pass (which recomputes the marked
+    rows) is exercised here."""
     p = small_params(app, nx, ny)
     out = []
     for mode in (_abi.FV_DIVISION_FMA, _abi.FV_DIVISION_EXACT):
@@ -322,11 +324,11 @@ def test_division_modes_give_the_same_results(app, nx, ny):
         assert same_values(a[f], b[f])
 
 
-def test_default_division_depends_on_the_grid():
+def test_default_division_is_exact_and_settable():
     small = Simulation(small_params(3, 300, 130))
     large = Simulation(small_params(3, 2048, 1024))
     try:
-        assert small.get_division() == _abi.FV_DIVISION_FMA
+        assert small.get_division() == _abi.FV_DIVISION_EXACT
         assert large.get_division() == _abi.FV_DIVISION_EXACT
         large.set_division(_abi.FV_DIVISION_FMA)
         assert large.get_division() == _abi.FV_DIVISION_FMA
