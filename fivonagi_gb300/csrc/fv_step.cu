@@ -634,6 +634,11 @@ template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 2) fixup_kernel(StepArgs a) {
   __shared__ float red[kWarps];
   __shared__ int sh[1];
+  // nothing marked (the usual case with exact division): one load and out;
+  // the finalize launch then reads the step's partials only
+  constexpr unsigned kItems = kFixRows / kFixItemRows;  // items per chunk
+  const unsigned n = __ldcg(a.fix) * kItems;
+  if (n == 0u) return;
   const Ctrl *ctl = a.ctrl;
   if (!attempt_active(ctl)) return;
   const float dt = __ldcg(&ctl->dt);
@@ -654,9 +659,6 @@ __global__ void __launch_bounds__(kThreads, 2) fixup_kernel(StepArgs a) {
   const int cpw = fix_chunks_per_window(ny);
   const long long bitmap_words = fix_bitmap_words((long long)a.nstrips * kWarps, ny);
   const uint32_t *list = a.fix + 4 + bitmap_words;
-  constexpr unsigned kItems = kFixRows / kFixItemRows;  // items per chunk
-  const unsigned n = __ldcg(a.fix) * kItems;
-  if (n == 0u) return;  // nothing marked: the finalize launch reads the step's partials only
   float cmax = 0.0f;
   bool neg = false;
   const unsigned nw = gridDim.x * kWarps;
