@@ -464,6 +464,9 @@ fv_status ensure_graph1(fv_handle *h) {
   ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, 1LL, std::numeric_limits<float>::infinity());
   int rc = (int)cudaGetLastError();
   if (rc == 0) rc = launch_attempt(h);
+  // and the control block back to the host, for the step's stats
+  if (rc == 0)
+    rc = (int)cudaMemcpyAsync(h->ctrl_host, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
   if (rc != 0) return fail(FV_CUDA_ERROR, "step launch during capture: %s", cudaGetErrorString((cudaError_t)rc));
   if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
@@ -1086,13 +1089,17 @@ fv_status fv_sync(fv_handle *h, fv_run_stats *out) {
 fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
   if (!h || nsteps < 0) return fail(FV_BAD_ARG, "bad argument");
   long long todo = nsteps;
+  bool have_ctrl = false;  // ctrl_host holds the control block after the launches
   if (nsteps == 1) {
     // one step, the call of a caller that reads every step's stats: the
-    // control-block set-up and the attempt as one graph launch
+    // control-block set-up, the attempt and the copy of the control block
+    // to the host as one graph launch
     fv_status s = ensure_graph1(h);
     if (s != FV_OK) return s;
     FV_CUDA(cudaGraphLaunch(h->graph1, h->stream));
+    FV_CUDA(cudaStreamSynchronize(h->stream));
     todo = 0;
+    have_ctrl = true;
   } else {
     ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nsteps,
                                               std::numeric_limits<float>::infinity());
@@ -1101,7 +1108,8 @@ fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
   for (;;) {
     fv_status s = todo > 0 ? enqueue_attempts(h, todo) : FV_OK;
     if (s != FV_OK) return s;
-    s = read_ctrl(h);
+    if (!have_ctrl) s = read_ctrl(h);
+    have_ctrl = false;
     if (s != FV_OK) return s;
     const Ctrl &c = *h->ctrl_host;
     if (c.status != 0 || c.remaining <= 0) break;
