@@ -1,46 +1,49 @@
 // fv_step.cu -- the fused time-step kernel for sm_103a.
 //
-// One launch performs one attempted step of the reference's loop body
-// (common/main.cu:310-635):
+// An attempt runs the reference's loop body (common/main.cu:310-635):
 //   boundary (app hook)  ->  y sweep  ->  x sweep  ->  CFL max  ->
-//   [accepted] diffusion, T += dt, n += 1  ->  dt update.
-// The reference runs this as ~34 kernel launches that pass 19 scratch
+//   [accepted] diffusion, T += dt, n += 1  ->  dt update,
+// as four launches: the ghost-frame pre-pass (the app hook's values of the
+// ghost cells), the step kernel, the fix-up kernel and a one-CTA finalize
+// kernel. The reference runs it as ~34 kernel launches that pass 19 scratch
 // grids through global memory (~750 B per cell-update) and 7 blocking
 // device-to-host copies. Here every intermediate lives in registers:
 //
-//  * Each warp owns a strip of 32 consecutive columns and streams up the
-//    grid one row per iteration. Lanes 3..28 produce output; the three
-//    lanes on each side are the x-halo the limiter and diffusion need.
+//  * Each warp streams a window of 32 consecutive columns up the grid, one
+//    row per iteration. Lanes 3..28 produce output; the three lanes on each
+//    side are the x-halo the limiter and diffusion need.
 //  * y sweep: a lane keeps the last rows of its own column (state, waves,
 //    first-order sums, correction fluxes) in registers, so each y interface
-//    is solved once per strip and each cell is updated two rows behind the
+//    is solved once per window and each cell is updated two rows behind the
 //    row being loaded.
 //  * x sweep: once a row of y-updated cells is ready, neighbouring columns
 //    are neighbouring lanes; the Riemann inputs, waves, dot products,
 //    fluctuations and correction fluxes move between lanes with warp
 //    shuffles.
-//  * diffusion (source): runs one row behind the x sweep, on registers.
+//  * diffusion (source): runs two rows behind the x sweep, on registers.
 //  * CFL: each lane keeps a running maximum over its output cells; warp
-//    shuffles and a CTA reduction produce one value per CTA, and the last
-//    CTA to finish (atomic counter) reduces those, accepts or rejects the
-//    step, and updates dt, T, n and the current-buffer index in device
-//    memory. A rejected step leaves the input buffer current, so the retry
-//    starts from the pre-step state.
+//    shuffles and a CTA reduction give one value per CTA, and the finalize
+//    kernel reduces those, accepts or rejects the step, and updates dt, T,
+//    n and the current-buffer index in device memory. A rejected step
+//    leaves the input buffer current, so the retry starts from the pre-step
+//    state.
 //
 // Work distribution: every warp streams a balanced share of the (window,
 // row) space, windows being the 26-column output spans, so every warp
 // streams the same number of rows; a share may span two windows.
 //
-// Division: the step kernel divides with Markstein's FMA sequence
-// (DivFma, fv_device.cuh), which equals IEEE division unless an operand is
-// tiny, huge or not finite. A warp that meets such an operand in an
-// iteration marks the rows that iteration can influence (chunks of
-// kFixRows rows of its window) and leaves their CFL and negative-eigenvalue
-// checks out; a fix-up kernel then recomputes the marked chunks from the
-// same input with exact division (IEEE division wherever FMA division's
-// conditions fail), overwriting their output, and its last CTA accepts or
-// rejects the attempt. Marked chunks are rare (the decaying
-// tails of a wave front), and the step kernel itself stays branch-free.
+// Division (fv_device.cuh): by default the step kernel divides exactly
+// (kStageExactDiv): DivExact for the quotients that can be subnormal, and
+// DivNormal, which flags a subnormal result, for the others. Stage -1
+// divides with Markstein's FMA sequence (DivFma) instead, which equals IEEE
+// division unless an operand is tiny, huge or not finite. Either way, a
+// warp that meets a flagged division in an iteration marks the rows that
+// iteration can influence (chunks of kFixRows rows of its window) and
+// leaves their CFL and negative-eigenvalue checks out; the fix-up kernel
+// then recomputes the marked chunks from the same input with DivExact (IEEE
+// division wherever even that flags), overwriting their output, before the
+// finalize kernel decides the attempt. Marked chunks are rare (none in
+// practice with exact division), and the step kernel stays branch-free.
 //
 // This file is compiled twice: FV_VARIANT_EXACT with --fmad=false (the
 // oracle's evaluation, bit for bit) and the fast variant with FMA
