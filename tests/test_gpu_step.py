@@ -337,3 +337,32 @@ def test_default_division_is_exact_and_settable():
     finally:
         small.close()
         large.close()
+
+
+def test_single_step_runs_match_a_multi_step_run_and_retry_rejections():
+    """fv_run(h, 1) runs as one captured graph with the control block's copy
+    to the host; a rejected attempt inside it is retried with separate
+    launches. Ten such calls equal one ten-step run, rejections included."""
+    p = small_params(2, 64, 32).replace(dtini=0.3)  # the first attempt is rejected
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    u = orc.get_state()
+    so = orc.run(10)
+    assert so["rejected"] >= 1
+    one = Simulation(p)
+    one.set_state(*u)
+    rejected = 0
+    for _ in range(10):
+        st = one.run(1)
+        assert st["accepted"] == 1
+        rejected += st["rejected"]
+    many = Simulation(p)
+    many.set_state(*u)
+    sm = many.run(10)
+    assert rejected == sm["rejected"] == so["rejected"]
+    a, b, o = one.get_state(), many.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(a[f], b[f]) and same_values(a[f], o[f])
+    assert np.float32(one.stats()["T"]) == np.float32(sm["T"]) == np.float32(so["T"])
+    one.close()
+    many.close()
