@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -397,41 +398,59 @@ __global__ void __launch_bounds__(128) adj_sweep_y_kernel(DevParams p, float dt,
     WaveAdj cp1, cp2, c0p;  // cp of the limiter reverses at j-2 and j-3, c0 of the one at j-2
     zero(cp1); zero(cp2); zero(c0p);
     Adj3 gap{0.f, 0.f, 0.f};  // ga of the solve at j-3
-    for (int j = j0 - 2; j <= j1 + 2; ++j) {
+    // Iteration j: the waves at interface j (always needed), the limiter's
+    // reverse at j-1 (needed from j = j0 on: the limiters at j0-1 .. j1+1
+    // feed the solves' reverses at j0 .. j1) and the solve's reverse at j-2
+    // (needed from j = j0+2 on). Three compile-time phases keep the loop
+    // body free of branches.
+    auto iterate = [&](int j, auto do_limiter, auto do_solve) {
+      constexpr bool kLimiter = decltype(do_limiter)::value;
+      constexpr bool kSolve = decltype(do_solve)::value;
       Adj3 s0, l0;
       load(j, s0, l0);
       const WaveN w0 = sweep_waves(s0, s1, two_bm1, dty, j >= 1 && j <= ny - 1);
-      const Adj3 mu1 = masked(l1, interior(p, i, j - 1)), mu2 = masked(l2, interior(p, i, j - 2));
-      const Adj3 mu3 = masked(l3, interior(p, i, j - 3));
-      // the limiter's reverse at interface j-1 (waves j-2, j-1, j)
       WaveAdj cm, c0, cp;
       zero(cm); zero(c0); zero(cp);
-      if (j - 1 >= 1 && j - 1 <= ny - 1)
-        correction_adj(w2, w1, w0, dty, dty * (mu1.q1 - mu2.q1), dty * (mu1.qn - mu2.qn), dty * (mu1.qt - mu2.qt),
-                       cm, c0, cp);
-      // the waves' adjoint at interface j-2 and the solve's reverse there
-      WaveAdj g = cp2;
-      add_to(g, c0p);
-      add_to(g, cm);
-      FluctAdj gf;
-      gf.am1 = -dty * mu3.q1; gf.am2 = -dty * mu3.qn; gf.am3 = -dty * mu3.qt;
-      gf.ap1 = -dty * mu2.q1; gf.ap2 = -dty * mu2.qn; gf.ap3 = -dty * mu2.qt;
+      if constexpr (kLimiter) {
+        // the limiter's reverse at interface j-1 (waves j-2, j-1, j)
+        const Adj3 mu1 = masked(l1, interior(p, i, j - 1)), mu2 = masked(l2, interior(p, i, j - 2));
+        if (j - 1 >= 1 && j - 1 <= ny - 1)
+          correction_adj(w2, w1, w0, dty, dty * (mu1.q1 - mu2.q1), dty * (mu1.qn - mu2.qn),
+                         dty * (mu1.qt - mu2.qt), cm, c0, cp);
+      }
       Adj3 ga{0.f, 0.f, 0.f}, gb{0.f, 0.f, 0.f};
-      if (j - 2 >= 1 && j - 2 <= ny - 1) riemann_adj(s2.q1, s2.qn, s2.qt, s3.q1, s3.qn, s3.qt, two_bm1, g, gf, ga, gb);
-      // row j-3: lo + ga (solve at j-3) + gb (solve at j-2)
-      const int r3 = j - 3;
-      if (col && r3 >= j0 && r3 < j1) {
-        float a1 = 0.f, an = 0.f, at = 0.f;
-        if (r3 >= 1) { a1 += gap.q1; an += gap.qn; at += gap.qt; }
-        if (r3 + 1 <= ny - 1) { a1 += gb.q1; an += gb.qn; at += gb.qt; }
-        store_local(li, false, size_t(i) + size_t(r3) * nx, Adj3{l3.q1 + a1, l3.qn + an, l3.qt + at});
+      if constexpr (kSolve) {
+        // the waves' adjoint at interface j-2 and the solve's reverse there
+        const Adj3 mu2 = masked(l2, interior(p, i, j - 2)), mu3 = masked(l3, interior(p, i, j - 3));
+        WaveAdj g = cp2;
+        add_to(g, c0p);
+        add_to(g, cm);
+        FluctAdj gf;
+        gf.am1 = -dty * mu3.q1; gf.am2 = -dty * mu3.qn; gf.am3 = -dty * mu3.qt;
+        gf.ap1 = -dty * mu2.q1; gf.ap2 = -dty * mu2.qn; gf.ap3 = -dty * mu2.qt;
+        if (j - 2 >= 1 && j - 2 <= ny - 1)
+          riemann_adj(s2.q1, s2.qn, s2.qt, s3.q1, s3.qn, s3.qt, two_bm1, g, gf, ga, gb);
+        // row j-3: lo + ga (solve at j-3) + gb (solve at j-2)
+        const int r3 = j - 3;
+        if (col && r3 >= j0 && r3 < j1) {
+          float a1 = 0.f, an = 0.f, at = 0.f;
+          if (r3 >= 1) { a1 += gap.q1; an += gap.qn; at += gap.qt; }
+          if (r3 + 1 <= ny - 1) { a1 += gb.q1; an += gb.qn; at += gb.qt; }
+          store_local(li, false, size_t(i) + size_t(r3) * nx, Adj3{l3.q1 + a1, l3.qn + an, l3.qt + at});
+        }
       }
       s3 = s2; s2 = s1; s1 = s0;
       l3 = l2; l2 = l1; l1 = l0;
       w2 = w1; w1 = w0;
       cp2 = cp1; cp1 = cp; c0p = c0;
       gap = ga;
-    }
+    };
+    const std::true_type on{};
+    const std::false_type off{};
+    int j = j0 - 2;
+    for (; j <= j0 - 1; ++j) iterate(j, off, off);
+    for (; j <= j0 + 1; ++j) iterate(j, on, off);
+    for (; j <= j1 + 2; ++j) iterate(j, on, on);
   }
 }
 
