@@ -169,7 +169,16 @@ __global__ void adj_record_kernel(const Ctrl *c, AdjRec *rec, int parity, float 
 }
 
 // Scalars of step n of the frozen schedule (0-based: the step from u_n).
-__global__ void adj_sched_kernel(Ctrl *c, const float *sched_dt, const float *sched_T, int n, int cur) {
+// With `fix` (the backward's replays, which run without the finalize
+// launch): also a zero fix-up header, and a negative eigenvalue met by the
+// previous replay counted in `rejected` before the flag is cleared.
+__global__ void adj_sched_kernel(Ctrl *c, const float *sched_dt, const float *sched_T, int n, int cur,
+                                 uint32_t *fix = nullptr) {
+  if (fix) {
+    fix[0] = 0u;
+    fix[1] = 0u;
+    if (c->neg_flag) c->rejected += 1;
+  }
   c->dt = sched_dt[n];
   c->T = sched_T[n];
   c->n = n;
@@ -870,6 +879,10 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   const int wthreads = w.ni * w.nj, wblocks = (wthreads + 255) / 256;
   double *g_amp = a->acc + 1, *g_ph = a->acc + 1 + nelem;
   FVA_CUDA(cudaMemsetAsync(g_amp, 0, 2 * size_t(nelem) * sizeof(double), a->stream));
+  // the replays count the negative eigenvalues they meet here (none, unless
+  // a replay differs from the recorded forward)
+  FVA_CUDA(cudaMemsetAsync(&a->ctrl->rejected, 0, sizeof(a->ctrl->rejected), a->stream));
+  FVA_CUDA(cudaMemsetAsync(&a->ctrl->neg_flag, 0, sizeof(a->ctrl->neg_flag), a->stream));
   const size_t bytes = 3 * a->stride * sizeof(float);
   // lambda_N: the loss gradient of the final state
   int lc = 0;  // lam[lc] holds lambda_n
@@ -890,11 +903,11 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
         in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
         out[f] = slot(a->seg, a->stride, n - seg0, f);
       }
-      adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0);
+      adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0, a->fix);
       StepArgs s = step_args(a, a->dp_replay, in, out);
       for (int st = 0; st < 3; ++st)
         for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = stage_grid(a, n - 1 - seg0, st, f);
-      const int rc = launch(a, s, kStageRecord);
+      const int rc = launch(a, s, kStageReplay);
       if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
     for (long long n = seg1; n > seg0; --n) {
@@ -924,6 +937,12 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
     FVA_CUDA(cudaGetLastError());
   }
   FVA_CUDA(cudaStreamSynchronize(a->stream));
+  {
+    Ctrl c;
+    FVA_CUDA(cudaMemcpy(&c, a->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+    if (c.rejected != 0 || c.neg_flag != 0)
+      return afail(FV_NEGATIVE_EIGENVALUE, "a replay of the recorded forward met a negative eigenvalue");
+  }
   FVA_CUDA(cudaMemcpy(grad_amp, g_amp, sizeof(double) * nelem, cudaMemcpyDeviceToHost));
   FVA_CUDA(cudaMemcpy(grad_phase, g_ph, sizeof(double) * nelem, cudaMemcpyDeviceToHost));
   return FV_OK;

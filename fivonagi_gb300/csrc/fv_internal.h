@@ -97,6 +97,10 @@ constexpr int kLaunchFrame = -3, kLaunchStep = -4, kLaunchFixFinal = -5;
 // with FMA division: the fix-up pass then meets only operands out of
 // range. Chosen by StepArgs::div_exact.
 constexpr int kStageExactDiv = -6;
+// kStageRecord without the finalize launch: the adjoint's replays follow a
+// frozen schedule, so there is nothing to decide. Their caller resets the
+// fix-up scratch's header before each one and checks the eigenvalue flag.
+constexpr int kStageReplay = -7;
 __host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }

@@ -977,9 +977,10 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
       finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;
     case kStageRecord:
+    case kStageReplay:
       step_kernel<kStageRecord><<<grid, block, 0, st>>>(a);
       fixup_kernel<kStageRecord><<<a.fix_blocks, block, 0, st>>>(a);
-      finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
+      if (stage == kStageRecord) finalize_kernel<<<1, kFinalizeThreads, 0, st>>>(a);
       break;
     case 0: step_kernel<0><<<grid, block, 0, st>>>(a); break;
     case 1: step_kernel<1><<<grid, block, 0, st>>>(a); break;
