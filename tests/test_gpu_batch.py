@@ -94,3 +94,25 @@ def test_a_failing_simulation_does_not_stop_the_others():
     assert all(same_values(g[f], r[f]) for f in range(3))
     b.close()
 
+
+
+def test_config3_instances_equal_the_plain_path():
+    """A dozen simulations from the batched workload's generator (sides from
+    256 to 2048, random beta, dissipation, amplitude and wavelength), at the
+    batch's default launch (eight waves of CTAs), against each simulation
+    run alone on the plain path (itself checked against the oracle)."""
+    plist = configs.batched(12, seed=3)
+    b = Batch(plist)
+    b.init_state()
+    st = b.run(30)
+    for k, p in enumerate(plist):
+        s = Simulation(p)
+        s.init_state()
+        ss = s.run(30)
+        assert st[k]["accepted"] == 30 and st[k]["rejected"] == ss["rejected"]
+        assert np.float32(st[k]["T"]) == np.float32(ss["T"])
+        g, r = b.get_state(k), s.get_state()
+        for f in range(3):
+            assert same_values(g[f], r[f]), f"simulation {k} ({p.nx}x{p.ny}) field {f}"
+        s.close()
+    b.close()
