@@ -252,10 +252,10 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       yo.vy = dp.x.div_r(u.u3, rr);
       yo.cy = 0.0f;
       // normal = u3: the normal velocity's quotients are the others (DivPair)
-      yo.ok = riemann<true>(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
+      yo.ok = riemann<true, DP::kSubsonic>(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
                             vx_m1, two_bm1, dty, yo.cy, yo.w, yo.f, dp.s, dp.x);
       yo.dr = wave_dots(w_m1, yo.w);
-      correction(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp.s);
+      correction<DP::kSubsonic>(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp.s);
     };
     auto x_chain = [&](auto &dp) {
       const float rho1 = s1_m3.u1 + 1.0f;
@@ -268,7 +268,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       Fluct fx;
       xo.cx = cy_m3;  // the x kernel starts from the cell's y value (fv.h:57)
       // transverse = u3: the transverse velocity's quotients are the others
-      xo.ok = riemann<false>(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m, two_bm1,
+      xo.ok = riemann<false, DP::kSubsonic>(rho1, s1_m3.u2, s1_m3.u3, vn1, vt1, rho1m, u2m, u3m, vn1m, vt1m, two_bm1,
                              dtx, xo.cx, wx, fx, dp.s, dp.x);
       WaveN wn;
       wn.w11 = shdn(wx.w11); wn.w21 = shdn(wx.w21); wn.w31 = shdn(wx.w31);
@@ -278,7 +278,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       Dots dlx;
       dlx.d1 = shup(drx.d1); dlx.d2 = shup(drx.d2); dlx.d3 = shup(drx.d3);
       float fx1, fx2, fx3;
-      correction(wx, dlx, drx, dtx, fx1, fx2, fx3, dp.s);
+      correction<DP::kSubsonic>(wx, dlx, drx, dtx, fx1, fx2, fx3, dp.s);
       const float amn1 = shdn(fx.am1), amn2 = shdn(fx.am2), amn3 = shdn(fx.am3);
       const float fxn1 = shdn(fx1), fxn2 = shdn(fx2), fxn3 = shdn(fx3);
       const bool in_x = col_int && r - 3 >= 2 && r - 3 <= ny - 3;
@@ -310,7 +310,9 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     // ---- Y results
     if constexpr (RY) {
       const float cy = (r <= 0) ? 0.0f : yo.cy;  // cfl = 0 on j == 0 (apps/na/fv.h:212-215)
-      neg = neg || (!yo.ok && !excl_y && out_lane && r >= y0 && r < y1 && r >= 1);
+      // (the subsonic solve flags tmp3 < 0 too, so the fix-up pass makes
+      // this check there)
+      if constexpr (!DP::kSubsonic) neg = neg || (!yo.ok && !excl_y && out_lane && r >= y0 && r < y1 && r >= 1);
       const float fn1 = ap1 + yo.f.am1, fn2 = ap2 + yo.f.am2, fn3 = ap3 + yo.f.am3;
       const int cyr = r - 2;  // row of the y update
       Cell3 s1 = s0_m2;
@@ -354,7 +356,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
     if constexpr (RX) {
       const int cxr = r - 3;
       const bool own_x = out_lane && cxr >= y0 && cxr < y1;
-      neg = neg || (!xo.ok && !excl_x && own_x && i >= 1);
+      if constexpr (!DP::kSubsonic) neg = neg || (!xo.ok && !excl_x && own_x && i >= 1);
       {
         // CFL of cell (i, r-3): its y and x interfaces; 0 on i == 0
         const float cell = (i == 0) ? 0.0f : xo.cx;

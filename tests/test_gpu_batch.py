@@ -116,3 +116,26 @@ def test_config3_instances_equal_the_plain_path():
             assert same_values(g[f], r[f]), f"simulation {k} ({p.nx}x{p.ny}) field {f}"
         s.close()
     b.close()
+
+
+def test_supersonic_instance_matches_oracle():
+    """The batch kernel's subsonic solve flags an instance's supersonic
+    interfaces for the batch fix-up pass: one step of patches moving at 0.9
+    is the oracle's bit for bit, beside an ordinary instance."""
+    plist = [small_params(2, 96, 48), small_params(0, 64, 32)]
+    u0 = _states(plist, seed=21)
+    u0[0][1][10:22, 20:40] += np.float32(0.9)
+    u0[0][2][26:40, 50:70] -= np.float32(0.9)
+    b = Batch(plist)
+    for k, u in enumerate(u0):
+        b.set_state(k, *u)
+    st = b.run(1)
+    for k, p in enumerate(plist):
+        o = OracleSim(p, np.float32, math="fvm")
+        o.set_state(*u0[k])
+        so = o.run(1)
+        assert so["rc"] == 0 and st[k]["accepted"] == 1 and st[k]["rejected"] == so["rejected"]
+        g, r = b.get_state(k), o.get_state()
+        for f in range(3):
+            assert same_values(g[f], r[f]), f"simulation {k} field {f}: rel L2 {rel_l2(g[f], r[f]):.3e}"
+    b.close()

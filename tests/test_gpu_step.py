@@ -366,3 +366,43 @@ def test_single_step_runs_match_a_multi_step_run_and_retry_rejections():
     assert np.float32(one.stats()["T"]) == np.float32(sm["T"]) == np.float32(so["T"])
     one.close()
     many.close()
+
+
+
+@pytest.mark.parametrize("app", [0, 2])
+@pytest.mark.parametrize("division", [_abi.FV_DIVISION_EXACT, _abi.FV_DIVISION_FMA])
+def test_supersonic_interfaces_match_oracle(app, division):
+    """The step kernel's solve assumes subsonic flow (L1 > 0 > L2) and flags
+    the interfaces where that fails; the fix-up pass redoes their rows with
+    the general solve. Patches moving at 0.9 (x) and -0.9 (y), where
+    tmp3 ~ 1 - v^2 puts sqrt(tmp3) ~ 0.44 below |tmp1| ~ 0.9, take that
+    path. The first step must be the oracle's bit for bit; the shocks the
+    patches' edges make then drive tmp3 below zero, and the negative
+    eigenvalue must be reported at the same step, with the same state."""
+    p = small_params(app, 96, 48)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    u1, u2, u3 = perturbed(orc.get_state(), 3, 1e-4)
+    u2[10:22, 20:40] += np.float32(0.9)
+    u3[26:40, 50:70] -= np.float32(0.9)
+    orc.set_state(u1, u2, u3)
+    sim = Simulation(p)
+    sim.set_state(u1, u2, u3)
+    sim.set_division(division)
+    so = orc.run(1)
+    assert so["rc"] == 0 and so["accepted"] == 1
+    sg = sim.run(1)
+    assert sg["accepted"] == 1 and sg["rejected"] == so["rejected"]
+    g, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
+    assert np.float32(sg["dt"]) == np.float32(so["dt"]) and np.float32(sg["T"]) == np.float32(so["T"])
+    so = orc.run(5)
+    assert so["rc"] == _abi.FV_NEGATIVE_EIGENVALUE
+    with pytest.raises(_abi.FvError) as e:
+        sim.run(5)
+    assert e.value.status == _abi.FV_NEGATIVE_EIGENVALUE
+    g, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
+    sim.close()
