@@ -175,9 +175,11 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   const int lane = threadIdx.x & (kLanes - 1);
   const int nx = p.nx, ny = p.ny;
   const int i = xw - kHalo + lane;
-  const bool col_ok = (i >= 0) && (i < nx);
+  // A window without ghost columns has all its 32 columns in [2, nx-3]
+  // (stream_window's test), so those column tests are constant there.
+  const bool col_ok = EDGE ? ((i >= 0) && (i < nx)) : true;
   const bool out_lane = col_ok && lane >= kHalo && lane < kLanes - kHalo;
-  const bool col_int = (i >= 2) && (i <= nx - 3);
+  const bool col_int = EDGE ? ((i >= 2) && (i <= nx - 3)) : true;
   const float dtx = dt / p.dx;
   const float dty = dt / p.dy;
   const float ddtx2 = p.diffdelta * dt / (p.dx * p.dx);
@@ -205,6 +207,17 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
   // ghost frame. Warps without ghost columns only meet ghost rows, which
   // are the same for the whole warp.
   auto load_raw = [&](int r, Cell3 &v) {
+    if constexpr (!EDGE) {
+      // interior rows of an interior window (a branch uniform over the
+      // warp): plain loads
+      if (r >= 2 && r < ny - 2) {
+        const int o = i + r * nx;
+        v.u1 = __ldg(i0 + o);
+        v.u2 = __ldg(i1 + o);
+        v.u3 = __ldg(i2 + o);
+        return;
+      }
+    }
     if (col_ok && r >= 0 && r < ny) {
       const bool gh = EDGE ? is_ghost(p, i, r) : (r <= 1 || r >= ny - 2);
       const int o = gh ? frame_index(ci, r, nx, ny) : ci + r * nx;

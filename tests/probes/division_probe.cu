@@ -1,13 +1,14 @@
 // Checks the step kernel's FMA division (fvgb::DivFma, fv_device.cuh)
 // against the GPU's IEEE-754 division.
 //
-//  1. Exhaustive: for every float b with 2^-125 <= |b| <= 2^24 the refined
-//     reciprocal DivFma::recip(b).y equals the IEEE quotient 1/b (condition
-//     (1) of the Markstein argument in fv_device.cuh).
+//  1. Exhaustive: for every float b with 2^-126 <= |b| <= 2^24 the refined
+//     reciprocal fvgb::refined_recip(b) equals the IEEE quotient 1/b
+//     (condition (1) of the Markstein argument in fv_device.cuh).
 //  2. Sampled div(): quotients over operand classes that straddle every
 //     bound of the safety check (dividends near 2^-100 and 2^39, divisors
 //     near 2^-85 and 2^24, powers of two with any dividend, zeros,
-//     subnormals, all-ones significands, solver-like magnitudes). Every
+//     subnormals, all-ones significands, solver-like magnitudes, divisors
+//     from zero through the subnormals to 2^-124). Every
 //     quotient the policy does not flag as unsafe must equal the IEEE
 //     quotient bit for bit (NaN matching NaN).
 //  3. Sampled DivExact::div() over the same classes, and DivExact::ratio()
@@ -55,8 +56,7 @@ __global__ void recip_all(unsigned e_lo, unsigned e_hi, unsigned long long *bad)
     const unsigned m = (unsigned)(k & 0x7fffff), s = (unsigned)((k >> 23) & 1);
     const unsigned e = e_lo + (unsigned)(k >> 24);
     const float b = __uint_as_float(s << 31 | e << 23 | m);
-    fvgb::DivFma d;
-    const float y = d.recip(b).y;
+    const float y = fvgb::refined_recip(b);
     local += (__float_as_uint(y) != __float_as_uint(1.0f / b)) ? 1 : 0;
   }
   if (local) atomicAdd(bad, local);
@@ -86,6 +86,7 @@ __device__ void operands(int mode, uint64_t h1, uint64_t h2, float &a, float &b)
       break;
     }
     case 12: { a = __uint_as_float((uint32_t)h1 & 0x807fffffu); b = ((h2 & 1) ? -1.0f : 1.0f) * ((h2 & 2) ? 2.0f : 1.0f); break; }  // tails: subnormal / +-1, +-2
+    case 14: a = rnd(h1, -149, -40); b = rnd(h2, -152, -125); break;           // zero, subnormal and 2^-126 divisors
     default: a = __uint_as_float((uint32_t)h1); b = __uint_as_float((uint32_t)h2); break;  // any bits
   }
 }
@@ -231,19 +232,20 @@ int main(int argc, char **argv) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
   const int grid = (sms > 0 ? sms : 152) * 8;
   int rc = 0;
-  // 1. every divisor of magnitude 2^-125 .. 2^24
+  // 1. every divisor of magnitude 2^-126 .. 2^24
   cudaMemset(cnt, 0, 2 * sizeof(unsigned long long));
-  recip_all<<<grid, 256>>>(127 - 125, 127 + 24, cnt);
+  recip_all<<<grid, 256>>>(127 - 126, 127 + 24, cnt);
   unsigned long long h[2] = {0, 0};
   cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
-  std::printf("recip_all %llu 0 %llu\n", (unsigned long long)(150ull << 24), h[0]);
+  std::printf("recip_all %llu 0 %llu\n", (unsigned long long)(151ull << 24), h[0]);
   if (h[0]) rc = 1;
   // 2. sampled quotients
-  const char *names[14] = {"general", "dividend_2^-100", "tiny_dividend", "dividend_2^39",
-                           "divisor_2^-85", "divisor_2^24", "subnormal_dividend", "zero_dividend",
-                           "ones_significand", "solver_like", "exact_quotients", "pow2_divisor",
-                           "tail_divisors", "everything"};
-  for (int mode = 0; mode < 14; ++mode) {
+  constexpr int kModes = 15;
+  const char *names[kModes] = {"general", "dividend_2^-100", "tiny_dividend", "dividend_2^39",
+                               "divisor_2^-85", "divisor_2^24", "subnormal_dividend", "zero_dividend",
+                               "ones_significand", "solver_like", "exact_quotients", "pow2_divisor",
+                               "tail_divisors", "everything", "divisor_below_2^-124"};
+  for (int mode = 0; mode < kModes; ++mode) {
     cudaMemset(cnt, 0, 2 * sizeof(unsigned long long));
     div_sample<<<grid, 256>>>(mode, 0x5eed0000ull + 7919ull * mode, per_mode, cnt, cnt + 1, ex);
     float e[4] = {0, 0, 0, 0};
@@ -255,7 +257,7 @@ int main(int argc, char **argv) {
     if (h[1]) rc = 1;
   }
   // 3. the fix-up pass's exact division
-  for (int mode = 0; mode < 14; ++mode) {
+  for (int mode = 0; mode < kModes; ++mode) {
     cudaMemset(cnt, 0, 2 * sizeof(unsigned long long));
     exact_sample<<<grid, 256>>>(mode, 0x4b1d0000ull + 7919ull * mode, per_mode / 4, cnt, cnt + 1, ex);
     float e[4] = {0, 0, 0, 0};
@@ -267,7 +269,7 @@ int main(int argc, char **argv) {
     if (h[1]) rc = 1;
   }
   // 3b. the exact-division step kernel's normal-quotient division
-  for (int mode = 0; mode < 14; ++mode) {
+  for (int mode = 0; mode < kModes; ++mode) {
     cudaMemset(cnt, 0, 2 * sizeof(unsigned long long));
     normal_sample<<<grid, 256>>>(mode, 0x90a10000ull + 7919ull * mode, per_mode / 4, cnt, cnt + 1, ex);
     float e[4] = {0, 0, 0, 0};

@@ -39,7 +39,7 @@ def test_fma_division_is_ieee_where_not_flagged(tmp_path):
         if len(f) >= 4 and f[1].isdigit():
             rows[f[0]] = (int(f[1]), int(f[2]), int(f[3]), line)
     assert out.returncode == 0, out.stdout + out.stderr
-    assert rows["recip_all"][0] == 150 << 24 and rows["recip_all"][2] == 0
+    assert rows["recip_all"][0] == 151 << 24 and rows["recip_all"][2] == 0
     for name, (n, flagged, bad, line) in rows.items():
         assert bad == 0, line
         assert flagged <= n
@@ -53,12 +53,18 @@ def test_fma_division_is_ieee_where_not_flagged(tmp_path):
     # the fix-up pass's exact division: checked on every class, and it
     # flags nothing in the classes the solver produces, tiny and subnormal
     # dividends included
-    assert sum(1 for k in rows if k.startswith("xdiv_")) == 14
+    assert sum(1 for k in rows if k.startswith("xdiv_")) == 15
     # the normal-quotient division: checked on every class (bad == 0 above);
     # it flags nothing where the solver's quotients are normal
-    assert sum(1 for k in rows if k.startswith("ndiv_")) == 14
+    assert sum(1 for k in rows if k.startswith("ndiv_")) == 15
     for name in ("solver_like", "dividend_2^-100", "exact_quotients"):
         assert rows["ndiv_" + name][1] == 0, rows["ndiv_" + name][3]
+    # zero and subnormal divisors reach the scaled-dividend divisions with
+    # no range test of their own: the NaN reciprocal flags them (bad == 0
+    # above), while divisors of 2^-126 .. 2^-124 pass unflagged
+    for pre in ("xdiv_", "ndiv_"):
+        n, flagged, _, line = rows[pre + "divisor_below_2^-124"]
+        assert 0 < flagged < n, line
     for name in ("solver_like", "tiny_dividend", "subnormal_dividend",
                  "dividend_2^-100", "tail_divisors", "exact_quotients"):
         assert rows["xdiv_" + name][1] == 0, rows["xdiv_" + name][3]
