@@ -194,7 +194,7 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
   if (e != cudaSuccess) return cleanup(bfail(FV_CUDA_ERROR, "batch allocation: %s", cudaGetErrorString(e)));
   b->stream = b->own_stream;
 
-  long long work = 0, fix_chunks = 0;
+  long long work = 0, cost = 0, fix_chunks = 0;
   int max_frame = 0;
   b->host_inst.resize(n);
   for (int k = 0; k < n; ++k) {
@@ -209,6 +209,9 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
     I.work_begin = work;
     I.work = (long long)windows * params[k].ny;
     work += I.work;
+    I.cost_begin = cost;
+    I.cost = ShareCost(params[k].nx, params[k].ny).total();
+    cost += I.cost;
     I.fix_base = fix_chunks;
     fix_chunks += (long long)windows * fix_chunks_per_window(params[k].ny);
     max_frame = std::max(max_frame, 4 * params[k].nx + 4 * (params[k].ny - 4));
@@ -231,6 +234,7 @@ fv_status fv_batch_create(int32_t n, const fv_params *params, fv_batch **out) {
   a.fix = b->fix;
   a.n = n;
   a.work = work;
+  a.cost = cost;
   a.fix_chunks = fix_chunks;
   a.max_frame = max_frame;
   // the fix-up launch: four CTAs per SM (its occupancy) take the marked chunks

@@ -14,6 +14,55 @@ constexpr int kLanes = 32;
 constexpr int kHalo = 3;
 constexpr int kWarpCols = kLanes - 2 * kHalo;  // 26
 
+#ifdef __CUDACC__
+#define FV_HD __host__ __device__ __forceinline__
+#else
+#define FV_HD inline
+#endif
+
+// A grid's work in cost order, by which the step kernels give every warp
+// an equal share of (window, row) pairs: window w costs kShareStart (the
+// loop's warm-up and drain, run again by the warp that enters it) plus ny
+// rows of kShareRow, or of kShareEdgeRow when it has ghost columns (w == 0
+// and w >= w_hi1). Measured on the focused beam, 4096x2048, against equal
+// rows per warp: 4.1% shorter attempts; edge rows weighted 1.25 or 1.75,
+// or starts of 2 rows, were slower.
+constexpr long long kShareRow = 16;
+constexpr long long kShareEdgeRow = 24;
+constexpr long long kShareStart = 6 * kShareRow;
+
+struct ShareCost {
+  long long ny, windows, w_hi1;  // w_hi1: first ghost-column window past 0
+  FV_HD ShareCost(long long nx, long long ny_) : ny(ny_) {
+    windows = (nx + kWarpCols - 1) / kWarpCols;
+    // window w has ghost columns when its 32 columns reach column 1 or
+    // column nx-2 (the step kernel's edge test): w == 0, or 26w + 28 >= nx - 2
+    const long long reach = nx - 2 - (kLanes - kHalo - 1);  // 26w >= reach
+    const long long w_hi = reach > 0 ? (reach + kWarpCols - 1) / kWarpCols : 0;
+    w_hi1 = w_hi > 1 ? w_hi : 1;
+  }
+  // cost of windows [0, w)
+  FV_HD long long prefix(long long w) const {
+    const long long edges = (w > 0 ? 1 : 0) + (w > w_hi1 ? w - w_hi1 : 0);
+    return w * (kShareStart + ny * kShareRow) + ny * (kShareEdgeRow - kShareRow) * edges;
+  }
+  FV_HD long long total() const { return prefix(windows); }
+  // (window * ny + row) of the first row at or after cost c; monotone in c,
+  // so consecutive cost ranges give consecutive row ranges
+  FV_HD long long pos(long long c) const {
+    if (c >= total()) return windows * ny;
+    long long w = c / (kShareStart + ny * kShareRow);  // >= the window of c
+    if (w >= windows) w = windows - 1;
+    while (w > 0 && prefix(w) > c) --w;                // at most the edge windows' extra cost
+    while (w + 1 < windows && prefix(w + 1) <= c) ++w;
+    const long long o = c - prefix(w) - kShareStart;
+    const long long u = (w == 0 || w >= w_hi1) ? kShareEdgeRow : kShareRow;
+    const long long r = o <= 0 ? 0 : (o + u - 1) / u;
+    return w * ny + (r < ny ? r : ny);
+  }
+};
+
+
 // Parameters the step kernel reads, already rounded to FP32 the way the
 // reference's `static const DATATYPEV` definitions round them.
 struct DevParams {
@@ -139,6 +188,8 @@ struct BatchInst {
   Ctrl *ctrl;
   int64_t work_begin;     // first window-row of this instance in the batch
   int64_t work;           // windows * ny (windows of kWarpCols output columns)
+  int64_t cost_begin;     // first cost unit of this instance in the batch
+  int64_t cost;           // ShareCost(nx, ny).total()
   int64_t fix_base;       // first chunk id of this instance in the fix-up scratch
 };
 
@@ -153,6 +204,7 @@ struct BatchArgs {
   int32_t n;
   int32_t nblocks;
   int64_t work;           // total window-rows
+  int64_t cost;           // total cost units (ShareCost)
   int64_t fix_chunks;     // total chunks over all instances
   int32_t max_frame;      // largest frame pre-pass work of an instance
   int32_t fix_blocks;     // CTAs of the fix-up launch

@@ -28,9 +28,11 @@
 //    leaves the input buffer current, so the retry starts from the pre-step
 //    state.
 //
-// Work distribution: every warp streams a balanced share of the (window,
-// row) space, windows being the 26-column output spans, so every warp
-// streams the same number of rows; a share may span two windows.
+// Work distribution: every warp streams an equal share of the launch's
+// cost, in (window, row) order, windows being the 26-column output spans.
+// A row of a window with ghost columns costs 1.5 rows of an interior one,
+// and each window start costs 6 rows (the warp that enters it runs the
+// loop's warm-up and drain again); a share may span two windows.
 //
 // Division (fv_device.cuh): by default the step kernel divides exactly
 // (kStageExactDiv): DivExact for the quotients that can be subnormal, and
@@ -606,14 +608,13 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   const int ny = a.p.ny;
   float cmax = 0.0f;
   bool neg = false;
-  // Each warp streams a balanced share of the (window, row) pairs, windows
-  // of kWarpCols output columns: every warp of the launch gets the same
-  // number of rows, whatever the last window's width.
-  const long long windows = (a.p.nx + kWarpCols - 1) / kWarpCols;
-  const long long W = windows * ny;
+  // Each warp streams the (window, row) pairs of an equal share of the
+  // launch's cost (ShareCost).
+  const ShareCost sc(a.p.nx, ny);
+  const long long C = sc.total();
   const long long G = (long long)a.nblocks * kWarps;
   const long long g = (long long)blockIdx.x * kWarps + warp;
-  const long long s0 = g * W / G, s1 = (g + 1) * W / G;
+  const long long s0 = sc.pos(g * C / G), s1 = sc.pos((g + 1) * C / G);
   for (long long pos = s0; pos < s1;) {
     const int win = (int)(pos / ny);
     const int y0 = (int)(pos - (long long)win * ny);
@@ -814,24 +815,28 @@ struct BatchMarker {
 // the simulation's buffers and parameters come from global memory, and at
 // four the kernel would spill (measured: three is faster).
 __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
-  // Each warp streams a balanced share of the batch's concatenated
-  // (simulation, window, row) space and folds its CFL maximum and
-  // negative-eigenvalue flag into each simulation it touched.
-  const long long W = b.work;
+  // Each warp streams the (simulation, window, row) triples of an equal
+  // share of the batch's cost (the simulations' ShareCost totals, end to
+  // end) and folds its CFL maximum and negative-eigenvalue flag into each
+  // simulation it touched.
+  const long long C = b.cost;
   const long long G = (long long)b.nblocks * kWarps;
   const long long g = (long long)blockIdx.x * kWarps + (threadIdx.x >> 5);
-  const long long s0 = g * W / G, s1 = (g + 1) * W / G;
-  int lo = 0, hi = b.n - 1;  // the simulation holding s0: last with work_begin <= s0
+  const long long c0 = g * C / G, c1 = (g + 1) * C / G;
+  int lo = 0, hi = b.n - 1;  // the simulation holding c0: last with cost_begin <= c0
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (b.inst[mid].work_begin <= s0) lo = mid; else hi = mid - 1;
+    if (b.inst[mid].cost_begin <= c0) lo = mid; else hi = mid - 1;
   }
   int k = lo;
-  long long pos = s0;
-  while (pos < s1 && k < b.n) {
+  long long c = c0;
+  while (c < c1 && k < b.n) {
     const BatchInst &I = b.inst[k];
-    const long long kb = I.work_begin, ke = kb + I.work;
-    const long long seg_end = s1 < ke ? s1 : ke;
+    const long long kb = I.cost_begin, ke = kb + I.cost;
+    const long long ce = c1 < ke ? c1 : ke;
+    const ShareCost sc(I.p.nx, I.p.ny);
+    // this simulation's window-rows [pos, seg_end)
+    const long long pos = sc.pos(c - kb), seg_end = sc.pos(ce - kb);
     if (pos < seg_end && attempt_active(I.ctrl)) {
       const DevParams &p = I.p;  // read in place (L1), not copied into registers
       const Ctrl *ctl = I.ctrl;
@@ -847,9 +852,8 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
       float cmax = 0.0f;
       bool neg = false;
       for (long long q = pos; q < seg_end;) {
-        const long long rel = q - kb;
-        const int win = (int)(rel / p.ny);
-        const int y0 = (int)(rel - (long long)win * p.ny);
+        const int win = (int)(q / p.ny);
+        const int y0 = (int)(q - (long long)win * p.ny);
         const long long left = seg_end - q;
         const int y1 = (int)((long long)y0 + left < p.ny ? (long long)y0 + left : p.ny);
         BatchMarker mk{b, k, -1};
@@ -867,7 +871,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
         if (wneg) atomicExch(b.neg + k, 1);
       }
     }
-    pos = seg_end;
+    c = ce;
     ++k;
   }
 }

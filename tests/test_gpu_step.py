@@ -19,10 +19,14 @@ pytestmark = pytest.mark.gpu
 APPS = [0, 1, 2, 3]
 SHAPES = [(64, 32), (100, 37), (8, 8), (300, 130), (27, 61)]
 TOL = 1e-5
-# Fast variant on the small cases: the FP32 rounding-noise floor of the
-# reference itself (a one-ulp change of T moves the 120-step result by this
-# much at these amplitudes, measured with the oracle) sets the bar.
-FAST_TOL = {0: 5e-4, 1: 5e-4, 2: 1e-4, 3: 1e-4}
+# Fast variant on the small cases: held to the accuracy of FP32 itself.
+# Against the oracle run in FP64, its relative L2 error per field after 120
+# steps may be at most FAST_FACTOR times that of the oracle run in FP32
+# (the reference's own rounding), plus FAST_FLOOR. The two FP32 runs round
+# differently and can sit on opposite sides of the FP64 result, so their
+# distance from each other is no bar: it reaches twice the FP32 error.
+FAST_FACTOR = 2.0
+FAST_FLOOR = 1e-6
 
 
 def _pair(app, nx, ny, exact=1, seed=0, scale=1e-4):
@@ -54,6 +58,7 @@ def test_stage_parity_exact(app, shape, stage):
 @pytest.mark.parametrize("exact", [1, 0])
 def test_run_parity(app, shape, exact):
     p, sim, orc = _pair(app, *shape, exact=exact)
+    u0 = orc.get_state()
     nsteps = 120
     sg = sim.run(nsteps)
     so = orc.run(nsteps)
@@ -62,12 +67,17 @@ def test_run_parity(app, shape, exact):
     assert sg["rejected"] == so["rejected"]
     g = sim.get_state()
     o = orc.get_state()
-    for f in range(3):
-        err = rel_l2(g[f], o[f])
-        if exact:
-            assert same_values(g[f], o[f]), f"field {f}: rel L2 {err:.3e}"
-        else:
-            assert err <= FAST_TOL[app], f"field {f}: rel L2 {err:.3e}"
+    if exact:
+        for f in range(3):
+            assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
+    else:
+        o64 = OracleSim(p, np.float64, math="fvm")
+        o64.set_state(*[x.astype(np.float64) for x in u0])
+        assert o64.run(nsteps)["rc"] == 0
+        t = o64.get_state()
+        for f in range(3):
+            err, ref = rel_l2(g[f], t[f]), rel_l2(o[f], t[f])
+            assert err <= FAST_FACTOR * ref + FAST_FLOOR, f"field {f}: rel L2 to FP64 {err:.3e}, oracle FP32 {ref:.3e}"
     if exact:
         assert np.float32(sg["dt"]) == np.float32(so["dt"])
         assert np.float32(sg["T"]) == np.float32(so["T"])
