@@ -46,6 +46,10 @@
 // division wherever even that flags), overwriting their output, before the
 // finalize kernel decides the attempt. Marked chunks are rare (none in
 // practice with exact division), and the step kernel stays branch-free.
+// The same flag carries the subsonic solve's assumption (L1 > 0 > L2 at
+// every interface; DivPair in fv_device.cuh): the step kernel skips the
+// speed-sign tests and the negative-eigenvalue check, and the fix-up
+// kernel's general solve redoes any rows where the assumption fails.
 //
 // This file is compiled twice: FV_VARIANT_EXACT with --fmad=false (the
 // oracle's evaluation, bit for bit) and the fast variant with FMA
