@@ -406,7 +406,9 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
                            ddty2 * (vy2_m6 - 2.0f * vy2_m5 + vy2_m4)
                      : s2_m5.u3;
         if (out_lane && cdr >= y0 && cdr < y1) {
-          if (STAGE < 0) {
+          if (STAGE < 0 && shx == 0 && shy == 0) {
+            store3(out, i + cdr * nx, o3);  // no shift this attempt (uniform)
+          } else if (STAGE < 0) {
             // moving window (moveDomain, common/main.cu:109-164): the new
             // cell (i - shx, j - shy) takes this cell's value, and a cell
             // whose source would lie past the far edge keeps its own value

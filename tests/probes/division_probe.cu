@@ -17,8 +17,9 @@
 //     The same for DivNormal::div(), which also flags subnormal quotients.
 //  4. Sampled ratio(): the limiter's quotient of a product-like dividend
 //     and a positive sum-of-squares divisor. Unflagged results equal the
-//     IEEE quotient, or, where that exceeds 2^59 in magnitude, have its sign
-//     and more than 2^59 in magnitude.
+//     IEEE quotient (DivNormal's as a value: a zero may have either sign),
+//     or, for DivFma where that exceeds 2^59 in magnitude, have its sign and
+//     more than 2^59 in magnitude.
 //
 // Prints one line per check: "<name> <count> <flagged> <mismatches>" and
 // exits 0 when no check found a mismatch.
@@ -197,6 +198,16 @@ __global__ void ratio_sample(int mode, uint64_t seed, long long n, unsigned long
       example[0] = a;
       example[1] = b;
       example[2] = qx;
+    }
+    // DivNormal's ratio leaves a zero quotient's sign out (the limiter
+    // gives +0 for either): equal to IEEE as a value, bit for bit otherwise
+    fvgb::DivNormal nr;
+    const float qn = nr.ratio(a, b);
+    if (!nr.unsafe() && !(qn == ref) && !(qn != qn && ref != ref)) {
+      ++bd;
+      example[0] = a;
+      example[1] = b;
+      example[2] = qn;
     }
     fvgb::DivFma d;
     const float q = d.ratio(a, b);
