@@ -45,7 +45,9 @@
 // then recomputes the marked chunks from the same input with DivExact (IEEE
 // division wherever even that flags), overwriting their output, before the
 // finalize kernel decides the attempt. Marked chunks are rare (none in
-// practice with exact division), and the step kernel stays branch-free.
+// practice with exact division), and the step kernel's arithmetic has no
+// branches: its only branches are uniform over a warp (interior-row loads,
+// the store of an attempt without a window shift, the rare marks).
 // The same flag carries the subsonic solve's assumption (L1 > 0 > L2 at
 // every interface; DivPair in fv_device.cuh): the step kernel skips the
 // speed-sign tests and the negative-eigenvalue check, and the fix-up
