@@ -873,6 +873,9 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
         q += y1 - y0;
       }
       for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+      // (with the subsonic solve of PairNormalExact neg stays false: a
+      // negative eigenvalue flags its rows, and the batch fix-up pass
+      // reports it)
       const bool wneg = __any_sync(0xffffffffu, neg);
       if ((threadIdx.x & 31) == 0) {
         atomicMax(b.cfl_bits + k, __float_as_uint(cmax));
