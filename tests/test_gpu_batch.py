@@ -139,3 +139,26 @@ def test_supersonic_instance_matches_oracle():
         for f in range(3):
             assert same_values(g[f], r[f]), f"simulation {k} field {f}: rel L2 {rel_l2(g[f], r[f]):.3e}"
     b.close()
+
+
+@pytest.mark.parametrize("blocks", [1, 2, 5])
+def test_few_ctas_batch_matches_oracle(blocks):
+    """A batch launched with 1-5 CTAs: each warp's share spans several
+    simulations and windows; every simulation is still the oracle's bit for
+    bit."""
+    plist = [small_params(app, nx, ny) for app, nx, ny in MIXED]
+    u0 = _states(plist, seed=31)
+    b = Batch(plist)
+    b.set_launch(blocks)
+    for k, u in enumerate(u0):
+        b.set_state(k, *u)
+    st = b.run(10)
+    for k, p in enumerate(plist):
+        o = OracleSim(p, np.float32, math="fvm")
+        o.set_state(*u0[k])
+        so = o.run(10)
+        assert st[k]["accepted"] == 10 and st[k]["rejected"] == so["rejected"]
+        g, r = b.get_state(k), o.get_state()
+        for f in range(3):
+            assert same_values(g[f], r[f]), f"simulation {k} field {f}: rel L2 {rel_l2(g[f], r[f]):.3e}"
+    b.close()

@@ -416,3 +416,20 @@ def test_supersonic_interfaces_match_oracle(app, division):
     for f in range(3):
         assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
     sim.close()
+
+
+@pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (0, 57, 41)])
+@pytest.mark.parametrize("blocks", [1, 3, 7])
+def test_few_ctas_match_oracle(app, nx, ny, blocks):
+    """With 1-7 CTAs each warp's share of the cost spans several windows,
+    edge windows included (ShareCost in fv_internal.h); the shares must
+    still tile every (window, row) once: bit for bit against the oracle."""
+    p, sim, orc = _pair(app, nx, ny)
+    sim.set_launch(blocks)
+    sg = sim.run(12)
+    so = orc.run(12)
+    assert so["rc"] == 0 and sg["accepted"] == so["accepted"] == 12 and sg["rejected"] == so["rejected"]
+    g, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
+    sim.close()
