@@ -114,8 +114,8 @@ struct Ctrl {
 // read by the step kernel in place of the state's own ghost cells. Layout:
 // rows j = 0, 1, ny-2, ny-1 (corners included) as four rows of nx, then the
 // left and right column pairs as [j][2] blocks of ny each.
-__host__ __device__ __forceinline__ int frame_cells(int nx, int ny) { return 4 * nx + 4 * ny; }
-__host__ __device__ __forceinline__ int frame_index(int i, int j, int nx, int ny) {
+FV_HD int frame_cells(int nx, int ny) { return 4 * nx + 4 * ny; }
+FV_HD int frame_index(int i, int j, int nx, int ny) {
   if (j <= 1) return j * nx + i;
   if (j >= ny - 2) return (j - ny + 4) * nx + i;
   if (i <= 1) return 4 * nx + 2 * j + i;
@@ -150,14 +150,14 @@ constexpr int kStageExactDiv = -6;
 // frozen schedule, so there is nothing to decide. Their caller resets the
 // fix-up scratch's header before each one and checks the eigenvalue flag.
 constexpr int kStageReplay = -7;
-__host__ __device__ __forceinline__ int fix_chunks_per_window(int ny) {
+FV_HD int fix_chunks_per_window(int ny) {
   return (ny + kFixRows - 1) / kFixRows;
 }
-__host__ __device__ __forceinline__ long long fix_bitmap_words(long long windows, int ny) {
+FV_HD long long fix_bitmap_words(long long windows, int ny) {
   return (windows * fix_chunks_per_window(ny) + 31) / 32;
 }
 // uint32 words of the whole fix-up scratch for `windows` warp windows
-__host__ __device__ __forceinline__ long long fix_scratch_words(long long windows, int ny) {
+FV_HD long long fix_scratch_words(long long windows, int ny) {
   return 4 + fix_bitmap_words(windows, ny) + windows * fix_chunks_per_window(ny);
 }
 
