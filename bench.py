@@ -24,9 +24,27 @@ y and x sweeps, CFL reduction and dt control, diffusion).
   cpu_baseline : the oracle's CPU restatement (FP32, OpenMP over rows, all
           host cores) on a bounded sample of the same grid.
 
+  error : relative L2 distance per field (u1, u2, u3) after the first
+          `--error-steps` steps from rest (500 by default): the exact GPU
+          path against the FP32 oracle evaluating the hooks' sin with the
+          library's correctly rounded functions (bit-identical: 0), against
+          the FP32 oracle with the host libm (the mode pinned to the
+          reference's own build), and against the FP64 oracle; the fast
+          variant against FP64.
+  batched, adjoint, fast : the other parts of the metric on the same run:
+          the config-3 batch against its simulations run one at a time
+          (`--steps` attempts each), the config-4 gradient cost (recorded
+          forward + backward over a plain forward, 4000 steps), and the FMA
+          variant at the headline size.
+  clocks : SM clock and throttle reasons sampled through NVML every
+          millisecond inside the timed region, with the whole run's samples
+          beside them.
+
 `--impl reference` times that CPU restatement alone (the reference's GPU
 code cannot be built with current toolkits; its arithmetic runs on the host
 through the restatement) and prints the same line with "impl": "reference".
+It loads none of this library: its parameter block is built in Python
+(`headline_params`, checked against the library's defaults by a CPU test).
 """
 from __future__ import annotations
 
@@ -39,6 +57,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
@@ -48,9 +68,36 @@ L2_BYTES = 129 * 1024 * 1024
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "step_kernel_focused_beam_4096x2048.traffic.json")
 
 
-def workload_params(exact: bool):
-    from fivonagi_gb300 import FV_APP_FOCUSED_BEAM, default_params
-    return default_params(FV_APP_FOCUSED_BEAM).replace(exact=1 if exact else 0)
+def headline_params(exact: bool = True):
+    """The focused-beam app's parameter block at 4096 x 2048, as
+    fv_default_params(FV_APP_FOCUSED_BEAM) gives it, built without loading
+    the library (the reference arm runs no product code)."""
+    from fivonagi_gb300._abi import FV_APP_FOCUSED_BEAM, FvParams
+
+    p = FvParams()
+    p.app = FV_APP_FOCUSED_BEAM
+    p.cfl_even_only, p.exact, p.max_retries = 1, 1 if exact else 0, 64
+    p.cflmax, p.cflwhish = 1.0, float(np.float32(90 / 100.0))
+    p.dtini = float(np.float32(0.005))
+    p.nx, p.ny = 4096, 2048
+    p.xmax, p.ymax = 4095.0 / 24.0, 2047.0 / 24.0
+    p.beta, p.diffdelta, p.ampl, p.frec = 3.5, 5e-5, 5e-3, 1.0
+    p.isp_f, p.aperture, p.center, p.ramp_periods, p.tide = 3000.0, 1024.0, 1024.0, 5.0, 0.0
+    return p
+
+
+def headline_config(params) -> dict:
+    """The `config` object of both arms' lines (identical keys and values)."""
+    return {
+        "workload": "focused-beam 4096x2048 FP32 (plain method, full size)",
+        "nx": params.nx, "ny": params.ny, "cells": params.nx * params.ny,
+        "source": "left edge, aperture 1024 cells centred on j=1024, focus 3000 cells, 24 cells per "
+                  "wavelength, Mach 5e-3 over a 5-period ramp",
+        "physics": "beta 3.5, dissipation 5e-5, CFL 0.9",
+        "start": "medium at rest",
+        "l2": "inputs larger than L2: each step reads one 100.7 MB state buffer and writes the other, "
+              "201 MB per step > 129 MB L2",
+    }
 
 
 def dist_env():
@@ -77,65 +124,137 @@ def replica_throughput(cells: int, steps_per_rank: int, world: int, ms: float) -
 
 
 class ClockSampler:
-    """nvidia-smi clock and throttle-reason samples during the timed region."""
+    """SM clock, power and throttle reasons of one GPU, read through NVML
+    (libnvidia-ml, read-only queries) every millisecond from a thread, so
+    that even a few-millisecond timed region gets samples; falls back to
+    nvidia-smi every 100 ms where NVML cannot be loaded. `begin()`/`end()`
+    bracket the timed region; samples outside it describe the whole run."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits (NVML's public header)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+    SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
-        self.proc = None
-        self.lines = []
+    def __init__(self, device_index: int, uuid: str | None = None, interval_s: float = 0.001):
+        self.index = device_index
+        self.uuid = uuid
+        self.interval = interval_s
+        self.samples = []  # (timed, sm_mhz, max_mhz, power_w, reasons bitmask or names)
+        self.timed = False
+        self.stop_flag = threading.Event()
         self.thread = None
+        self.proc = None
+        self.source = None
 
-    def start(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except (FileNotFoundError, OSError):
-            self.proc = None
-            return
-        self.thread = threading.Thread(target=self._read, daemon=True)
-        self.thread.start()
+    def _nvml(self):
+        import ctypes as C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = C.c_void_p()
+        rc = -1
+        if self.uuid:
+            u = self.uuid if self.uuid.startswith("GPU-") else "GPU-" + self.uuid
+            rc = lib.nvmlDeviceGetHandleByUUID(u.encode(), C.byref(h))
+        if rc != 0:
+            rc = lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h))
+        if rc != 0:
+            raise OSError("no NVML handle")
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, get_reasons
 
-    def _read(self):
+    def _run_nvml(self, lib, h, get_reasons):
+        import ctypes as C
+        clk, mx, pw, rs = C.c_uint(), C.c_uint(), C.c_uint(), C.c_ulonglong()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))  # NVML_CLOCK_SM
+        while not self.stop_flag.is_set():
+            ok = lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0
+            lib.nvmlDeviceGetPowerUsage(h, C.byref(pw))
+            get_reasons(h, C.byref(rs))
+            if ok:
+                self.samples.append((self.timed, float(clk.value), float(mx.value), pw.value / 1000.0,
+                                     int(rs.value)))
+            time.sleep(self.interval)
+
+    def _run_smi(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
-
-    def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        if self.thread:
-            self.thread.join(timeout=2)
-        sm, smax, reasons, power = [], [], set(), []
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-                power.append(float(parts[3]))
+                sm, smax, pw = float(parts[1]), float(parts[2]), float(parts[3])
             except ValueError:
                 continue
-            for name, val in zip(names, parts[5:9]):
-                if val.lower() == "active":
-                    reasons.add(name)
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            reasons = {n for n, v in zip(names, parts[5:9]) if v.lower() == "active"}
+            self.samples.append((self.timed, sm, smax, pw, reasons))
+
+    def start(self):
+        try:
+            lib, h, get_reasons = self._nvml()
+            self.source = "nvml, 1 ms"
+            self.thread = threading.Thread(target=self._run_nvml, args=(lib, h, get_reasons), daemon=True)
+        except (OSError, AttributeError):
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.SMI_FIELDS}",
+                     "--format=csv,noheader,nounits", "-lms", "100"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            except (FileNotFoundError, OSError):
+                return
+            self.source = "nvidia-smi, 100 ms"
+            self.thread = threading.Thread(target=self._run_smi, daemon=True)
+        self.thread.start()
+
+    def begin(self):
+        self.timed = True
+
+    def end(self):
+        self.timed = False
+
+    def _names(self, r) -> set:
+        if isinstance(r, set):
+            return r
+        return {name for bit, name in self.REASONS.items() if r & bit}
+
+    def stop(self) -> dict:
+        self.stop_flag.set()
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no clock samples (NVML and nvidia-smi "
+                                                                       "unavailable)"], "samples": 0}
+        timed = [x for x in self.samples if x[0]]
+        # the run's samples under load: power above the idle level of the run
+        pmax = max(x[3] for x in self.samples)
+        loaded = [x for x in self.samples if x[3] >= 0.5 * pmax]
+        use = timed or loaded
+        reasons = set()
+        for x in use:
+            reasons |= self._names(x[4])
+        run_reasons = set()
+        for x in loaded:
+            run_reasons |= self._names(x[4])
         return {
-            "sm_mhz": statistics.median(sm) if sm else None,
-            "sm_max_mhz": max(smax) if smax else None,
-            "power_w_max": max(power) if power else None,
-            "samples": len(sm),
+            "sm_mhz": statistics.median(x[1] for x in use),
+            "sm_max_mhz": max(x[2] for x in self.samples),
+            "power_w_max": pmax,
+            "samples": len(timed),
             "reasons": sorted(reasons),
+            "window": "timed region" if timed else "whole run under load (no sample inside the timed region)",
+            "source": self.source,
+            "run": {"samples": len(self.samples), "samples_under_load": len(loaded),
+                    "sm_mhz_median_under_load": statistics.median(x[1] for x in loaded) if loaded else None,
+                    "reasons": sorted(run_reasons)},
         }
 
 
@@ -161,8 +280,6 @@ def profiled_figures():
 
 def cpu_sample(params, seconds: float, max_steps: int):
     """The oracle (FP32 CPU restatement) on the full grid, bounded in time."""
-    import numpy as np
-
     from oracle import oracle
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
@@ -191,7 +308,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    params = workload_params(exact=True)
+    params = headline_params(exact=True)
     res = cpu_sample(params, seconds=25.0, max_steps=max(1, args.steps))
     line = {
         "impl": "reference",
@@ -206,9 +323,9 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "focused-beam 4096x2048 FP32 (plain method, full size)",
-                   "nx": params.nx, "ny": params.ny, "runs": "CPU restatement of the reference "
-                   "arithmetic on the host cores (the reference's CUDA does not build on current toolkits)"},
+        "config": headline_config(params),
+        "runs": "the CPU restatement of the reference's arithmetic on all host cores (the reference's CUDA "
+                "does not build on current toolkits)",
         "cpu_baseline": {"kind": res["kind"], "cores": res["cores"], "sample": res["sample"],
                          "value": res["value"], "unit": res["unit"]},
         "e2e": {"value": res["value"], "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
@@ -218,10 +335,152 @@ def run_reference(args):
     return 0
 
 
+def rel_l2_fields(a, b) -> list:
+    """Relative L2 distance of each field of state a from state b."""
+    out = []
+    for x, y in zip(a, b):
+        x = np.asarray(x, np.float64)
+        y = np.asarray(y, np.float64)
+        den = float(np.sqrt(np.sum(y * y)))
+        num = float(np.sqrt(np.sum((x - y) ** 2)))
+        out.append(num / den if den > 0 else num)
+    return out
+
+
+def error_report(params, nsteps: int) -> dict:
+    """FP32 GPU error of the headline workload after `nsteps` accepted steps
+    from rest, against the FP32 oracle in both of its transcendental modes
+    and against the FP64 oracle; the fast (FMA) variant against FP64."""
+    from fivonagi_gb300 import Simulation
+    from oracle import oracle
+
+    oracle.set_threads(os.cpu_count() or 1)
+    gpu = {}
+    for name, exact in (("exact", 1), ("fast", 0)):
+        sim = Simulation(params.replace(exact=exact))
+        sim.init_state()
+        sim.run(nsteps)
+        gpu[name] = sim.get_state()
+        sim.close()
+    ref = {}
+    for name, dtype, math in (("fvm32", np.float32, "fvm"), ("libm32", np.float32, "libm"),
+                              ("libm64", np.float64, "libm")):
+        o = oracle.OracleSim(params, dtype, math=math)
+        o.init_state()
+        o.run(nsteps)
+        ref[name] = o.get_state()
+        o.close()
+    exact_bits = all(np.array_equal(g, r) for g, r in zip(gpu["exact"], ref["fvm32"]))
+    return {
+        "steps": nsteps,
+        "fields": ["u1", "u2", "u3"],
+        "metric": "relative L2 per field after the steps, from rest",
+        "vs_fp32_oracle": rel_l2_fields(gpu["exact"], ref["fvm32"]),
+        "bit_identical_to_fp32_oracle": bool(exact_bits),
+        "vs_libm_oracle": rel_l2_fields(gpu["exact"], ref["libm32"]),
+        "vs_fp64": rel_l2_fields(gpu["exact"], ref["libm64"]),
+        "libm_fp32_oracle_vs_fp64": rel_l2_fields(ref["libm32"], ref["libm64"]),
+        "fast_vs_fp64": rel_l2_fields(gpu["fast"], ref["libm64"]),
+        "oracles": "fvm32: FP32 restatement with the hooks' sin from the library's correctly rounded "
+                   "functions (what the GPU computes); libm32: FP32 with the host libm (the mode pinned "
+                   "to the reference's own headers built on the host); libm64: FP64",
+    }
+
+
+def time_plain(params, blocks, division, steps, warmup, stream=None, sampler=None):
+    """Device time of `steps` back-to-back attempts of the headline workload
+    (CUDA events on the handle's stream)."""
+    from fivonagi_gb300 import Simulation
+
+    sim = Simulation(params)
+    sim.set_launch(blocks)
+    sim.set_division(division)
+    sim.init_state()
+    if stream is not None:
+        sim.set_stream(stream)
+    if warmup:
+        sim.run(warmup)
+    if sampler is not None:
+        sampler.begin()
+    ms = sim.time_run(steps)
+    if sampler is not None:
+        sampler.end()
+    st = sim.sync()
+    return sim, ms, st
+
+
+def fast_report(args, cells) -> dict:
+    """The FMA-contracted variant at the headline size, autotuned."""
+    from fivonagi_gb300 import autotune
+
+    p = headline_params(exact=False)
+    blocks, division = autotune.tune(p)
+    sim, ms, st = time_plain(p, blocks, division, args.steps, args.warmup)
+    sim.close()
+    return {"value": cells * st["accepted"] / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+            "ms_per_step": ms / max(1, st["accepted"]), "steps": args.steps,
+            "variant": "fast: FMA contraction (not bit-identical; held to FP32 accuracy, see error.fast_vs_fp64)"}
+
+
+def batched_report(args) -> dict:
+    """Config 3: 64 focused-beam simulations of uneven sizes and physics in
+    the batched launch, against the same simulations one at a time with the
+    plain path (autotuned per grid); `--steps` attempts each."""
+    from fivonagi_gb300 import Batch, Simulation, autotune, configs
+
+    plist = configs.batched(args.instances, seed=args.seed, exact=1)
+    cells = [p.nx * p.ny for p in plist]
+    b = Batch(plist)
+    b.init_state()
+    b.run(max(args.warmup, 3))
+    ms_batch = b.time_run(args.steps)
+    st = b.sync()
+    acc = [x["accepted"] for x in st]
+    b.close()
+    batched = sum(c * a for c, a in zip(cells, acc)) / (ms_batch * 1e-3) / 1e9
+    ms_seq, work_seq = 0.0, 0
+    for p in plist:
+        blocks, division = autotune.tune(p, steps=20)
+        sim = Simulation(p)
+        sim.set_launch(blocks)
+        sim.set_division(division)
+        sim.init_state()
+        sim.run(max(args.warmup, 3))
+        ms_seq += sim.time_run(args.steps)
+        work_seq += p.nx * p.ny * sim.sync()["accepted"]
+        sim.close()
+    sequential = work_seq / (ms_seq * 1e-3) / 1e9
+    return {"value": batched, "unit": "Gcell-updates/s", "sequential": sequential,
+            "ratio": batched / sequential, "instances": len(plist), "cells_per_step": sum(cells),
+            "steps": args.steps, "ms_per_attempt": ms_batch / args.steps,
+            "workload": f"{len(plist)} focused-beam simulations, sides from {list(configs.SIDES)} drawn "
+                        f"independently for x and y, random physics, seed {args.seed}"}
+
+
+def adjoint_report(args) -> dict:
+    """Config 4: the gradient of the windowed loss of the phased array
+    (1024x1024, 4000 steps) with respect to its 256 element weights; cost
+    of one gradient (recorded forward + backward) over a plain forward."""
+    from fivonagi_gb300 import _abi
+
+    p = _abi.default_params("phased-array")
+    nsteps = args.adjoint_steps or 4000
+    warm = min(200, nsteps)
+    _time_design(p, *_adjoint_case(p, (700, 512), warm, args.seed), warm)  # first launches
+    amp, ph, win = _adjoint_case(p, (700, 512), nsteps, args.seed)
+    r = _time_design(p, amp, ph, win, nsteps)
+    return {"forward_s": r["t_plain"], "recorded_forward_s": r["t_fwd"], "backward_s": r["t_bwd"],
+            "gradient_over_forward": (r["t_fwd"] + r["t_bwd"]) / r["t_plain"],
+            "backward_over_forward": r["t_bwd"] / r["t_plain"], "gradients_per_s": 1.0 / (r["t_fwd"] + r["t_bwd"]),
+            "steps": nsteps, "adjoint_memory_gb": r["mem"] / 1e9,
+            "workload": "phased array 1024x1024, 128 elements x (amplitude, phase), loss = mean u1^2 over a "
+                        f"32x32 window at (700, 512) over the last 500 steps, checkpoint every ceil(sqrt(N)) "
+                        f"steps, seed {args.seed}"}
+
+
 def run_gpu(args):
     import ctypes as C
 
-    import numpy as np
     import torch
 
     from fivonagi_gb300 import Simulation, _abi, autotune
@@ -233,8 +492,14 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     exact = not args.fast
-    params = workload_params(exact)
+    params = headline_params(exact)
     cells = params.nx * params.ny
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except (AttributeError, RuntimeError):
+        uuid = None
+    sampler = ClockSampler(local, uuid)
+    sampler.start()
 
     # ---- launch shape and division from the autotuner (cached; outside every
     # timed region), or as given (--blocks/--division: few launches before a
@@ -247,33 +512,17 @@ def run_gpu(args):
         if args.division != "default":
             division = DIVISIONS[args.division]
 
-    # ---- device-timed throughput (state resident in HBM)
-    sim = Simulation(params)
-    sim.set_launch(blocks)
-    sim.set_division(division)
-    division_used = "exact" if sim.get_division() == _abi.FV_DIVISION_EXACT else "fma"
-    sim.init_state()
+    # ---- device-timed throughput (state resident in HBM): K back-to-back
+    # attempts between CUDA events on the solver's stream
     stream = torch.cuda.Stream(device=dev)
-    sim.set_stream(stream.cuda_stream)
-    if args.warmup:
-        sim.run(args.warmup)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    sampler = ClockSampler(local)
-    sampler.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    sim.launch_attempts(args.steps)
-    ev1.record(stream)
-    stream.synchronize()
-    st = sim.sync()
+    sim, ms, st = time_plain(params, blocks, division, args.steps, args.warmup, stream.cuda_stream, sampler)
+    division_used = "exact" if sim.get_division() == _abi.FV_DIVISION_EXACT else "fma"
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
     if world > 1:
         ms = max_over_ranks(ms, dev)
     accepted = int(st["accepted"])
@@ -286,13 +535,7 @@ def run_gpu(args):
     for _ in range(5):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sim.launch_attempts(1)
-        e1.record(stream)
-        stream.synchronize()
-        flushed.append(e0.elapsed_time(e1))
+        flushed.append(sim.time_run(1))
     sim.sync()
     del flush
     flushed_ms = statistics.median(flushed)
@@ -326,16 +569,14 @@ def run_gpu(args):
     if world > 1:
         e2e_s = max_over_ranks(e2e_s, dev)
     state_bytes = 3 * cells * 4
-    ctrl_bytes = C.sizeof(_abi.FvRunStats)
     e2e = {
         "value": replica_throughput(cells, e2e_steps, world, e2e_s * 1e3),
         "unit": "Gcell-updates/s",
         "steps": e2e_steps,
         "h2d_bytes_per_step": state_bytes / e2e_steps,
-        "d2h_bytes_per_step": state_bytes / e2e_steps + 88,
+        "d2h_bytes_per_step": state_bytes / e2e_steps + C.sizeof(_abi.FvRunStats),
         "calls": "fv_set_state(pinned host) + steps x fv_run(1) (sync, stats read back) + fv_get_state(pinned host)",
     }
-    del ctrl_bytes
 
     peak, peak_kind = measured_peak()
     alg_bytes = ALG_BYTES_PER_CELL * cells
@@ -349,6 +590,8 @@ def run_gpu(args):
         "frac": achieved / peak,
         "peak_source": f"hbm_gbs, {peak_kind} (MEASURED_PEAKS.json); of measured",
         "traffic": prof.get("bytes_per_launch"),
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch "
+                          "(profiles/step_kernel_focused_beam_4096x2048.md)",
         "kernel": "step_kernel (fused y/x sweeps, CFL, diffusion)",
         "bytes_per_launch": alg_bytes,
         "launch_ms": step_kernel_ms,
@@ -360,6 +603,7 @@ def run_gpu(args):
                   "ipc": prof.get("ipc_active"), "ipc_peak": prof.get("ipc_peak"),
                   "issue_slots_busy": prof.get("issue_slots_busy"),
                   "warp_instructions_per_launch": prof.get("warp_instructions_per_launch"),
+                  "thread_instructions_per_cell": prof.get("thread_instructions_per_cell"),
                   "source": "ncu --set full, profiles/step_kernel_focused_beam_4096x2048.md"},
     }
 
@@ -376,27 +620,30 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": "focused-beam 4096x2048 FP32 (plain method, full size)",
-            "nx": params.nx, "ny": params.ny, "cells": cells,
+        "config": headline_config(params),
+        "run": {
             "variant": "exact (no FMA contraction; bit-identical to the oracle)" if exact else "fast (FMA)",
-            "cfl_target": params.cflwhish, "accepted": accepted, "rejected": int(st["rejected"]),
-            "T_end": st["T"],
-            "l2": "inputs larger than L2: each step reads one 100.7 MB state buffer and writes the "
-                  "other, 201 MB per step > 129 MB L2; attempt_ms_l2_flushed is one step after "
-                  "writing 258 MB",
+            "accepted": accepted, "rejected": int(st["rejected"]), "T_end": st["T"],
             "parallelism": "replicas" if world > 1 else "single GPU",
-            "ctas_per_launch": blocks,
-            "step_division": division_used,
+            "ctas_per_launch": blocks, "step_division": division_used,
+            "attempt_ms_l2_flushed": flushed_ms,
         },
         "roofline": roofline,
         "e2e": e2e,
         # per attempt: ghost-frame pre-pass, step, fix-up, finalize
         "gpu_launches": 4 * (accepted + int(st["rejected"])),
-        "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.headline_only:
+        line["fast"] = fast_report(args, cells)
+        line["batched"] = batched_report(args)
+        line["adjoint"] = adjoint_report(args)
+    line["clocks"] = sampler.stop()
+    if rank == 0 and world == 1 and args.error_steps > 0:
+        line["error"] = error_report(params, args.error_steps)
+        if "fast" in line:
+            line["fast"]["err_vs_fp64"] = line["error"]["fast_vs_fp64"]
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(params, seconds=args.cpu_seconds, max_steps=50)
+        line["cpu_baseline"] = cpu_sample(params, seconds=args.cpu_seconds, max_steps=200)
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
@@ -405,82 +652,40 @@ def run_gpu(args):
 
 
 def run_batched(args):
-    """Config 3: n focused-beam simulations of uneven sizes and physics,
-    stepped by the batched launch, against the same simulations run one at a
-    time with the plain path. Both legs are device-timed with CUDA events."""
+    """Config 3 alone: n focused-beam simulations of uneven sizes and
+    physics, stepped by the batched launch, against the same simulations
+    run one at a time with the plain path. Both legs are device-timed with
+    CUDA events on their handle's stream."""
     import torch
 
-    from fivonagi_gb300 import Batch, Simulation, autotune, configs
+    from fivonagi_gb300 import configs
 
-    rank, world, local = dist_env()
+    _, _, local = dist_env()
     torch.cuda.set_device(local)
-    plist = configs.batched(args.instances, seed=args.seed, exact=0 if args.fast else 1)
-    cells = [p.nx * p.ny for p in plist]
-    steps = args.steps
-    stream = torch.cuda.Stream()
-
-    # ---- batched: one launch per attempt of every simulation
-    b = Batch(plist)
-    b.set_stream(stream.cuda_stream)
-    b.init_state()
-    b.run(max(args.warmup, 3))
-    torch.cuda.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    b.launch_attempts(steps)
-    e1.record(stream)
-    stream.synchronize()
+    r = batched_report(args)
     clocks = sampler.stop()
-    st = b.sync()
-    ms_batch = e0.elapsed_time(e1)
-    acc = [s["accepted"] for s in st]
-    b.close()
-    batched_rate = sum(c * a for c, a in zip(cells, acc)) / (ms_batch * 1e-3) / 1e9
-
-    # ---- sequential: each simulation alone with the plain path, same steps
-    ms_seq = 0.0
-    acc_seq = 0
-    for p in plist:
-        sim = Simulation(p)
-        b, m = autotune.tune(p, steps=20)
-        sim.set_launch(b)
-        sim.set_division(m)
-        sim.set_stream(stream.cuda_stream)
-        sim.init_state()
-        sim.run(max(args.warmup, 3))
-        e0.record(stream)
-        sim.launch_attempts(steps)
-        e1.record(stream)
-        stream.synchronize()
-        s1 = sim.sync()
-        ms_seq += e0.elapsed_time(e1)
-        acc_seq += p.nx * p.ny * s1["accepted"]
-        sim.close()
-    seq_rate = acc_seq / (ms_seq * 1e-3) / 1e9
     line = {
         "metric": "Gcell-updates/s (batched, aggregate)",
-        "value": batched_rate,
+        "value": r["value"],
         "unit": "Gcell-updates/s",
         "n_gpus": 1,
-        "steps": steps,
+        "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": ms_batch / steps,
+        "ms_per_step": r["ms_per_attempt"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{len(plist)} focused-beam simulations, sides from {list(configs.SIDES)}, "
-                               f"seed {args.seed}", "cells_per_step": sum(cells),
-                   "variant": "fast (FMA)" if args.fast else "exact"},
-        "sequential_plain_path": {"value": seq_rate, "unit": "Gcell-updates/s", "ms_total": ms_seq},
-        "batched_over_sequential": batched_rate / seq_rate,
+        "config": {"workload": r["workload"], "cells_per_step": r["cells_per_step"],
+                   "sides": list(configs.SIDES), "variant": "exact"},
+        "sequential_plain_path": {"value": r["sequential"], "unit": "Gcell-updates/s"},
+        "batched_over_sequential": r["ratio"],
         "clocks": clocks,
         # per attempt: ghost-frame pre-pass, batch step, batch fix-up, batch finalize
-        "gpu_launches": 4 * steps,
+        "gpu_launches": 4 * args.steps,
     }
     print(json.dumps(line))
     return 0
@@ -686,6 +891,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true", help="leave out the CPU-baseline leg")
+    ap.add_argument("--error-steps", type=int, default=500,
+                    help="plain workload: steps from rest for the error object (0 leaves it out)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="plain workload: leave out the fast, batched and adjoint objects")
     ap.add_argument("--workload", choices=["plain", "batched", "adjoint", "designs"], default="plain",
                     help="plain: focused beam 4096x2048; batched: config-3 batch vs sequential; "
                          "adjoint: config-4 gradient; designs: config-5 gradients")

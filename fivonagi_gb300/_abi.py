@@ -215,6 +215,8 @@ PROTOTYPES = {
     "fv_run_until": (C.c_int, [_P, C.c_double, C.POINTER(FvRunStats)]),
     "fv_launch_attempts": (C.c_int, [_P, C.c_int64]),
     "fv_time_attempts": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "fv_time_run": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
+    "fv_device_name": (C.c_int, [C.c_char_p, C.c_int32]),
     "fv_set_division": (C.c_int, [_P, C.c_int32]),
     "fv_get_division": (C.c_int, [_P, _P]),
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
@@ -230,6 +232,7 @@ PROTOTYPES = {
     "fv_batch_run": (C.c_int, [_P, C.c_int64, C.POINTER(FvRunStats)]),
     "fv_batch_launch_attempts": (C.c_int, [_P, C.c_int64]),
     "fv_batch_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_batch_time_run": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_float)]),
     "fv_batch_set_launch": (C.c_int, [_P, C.c_int32]),
     "fv_batch_get_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "fv_step_noalloc": (C.c_int, [C.POINTER(FvParams), _P, _P, _P, _P, _P, _P, C.c_double, C.c_double,
@@ -290,3 +293,11 @@ def default_params(app: int | str) -> FvParams:
     p = FvParams()
     check(lib.fv_default_params(app, C.byref(p)), "fv_default_params")
     return p
+
+
+def device_name() -> str:
+    """The current CUDA device's name, from the library."""
+    lib = load_library()
+    buf = C.create_string_buffer(256)
+    check(lib.fv_device_name(buf, len(buf)), "fv_device_name")
+    return buf.value.decode()

@@ -45,12 +45,11 @@ def _store(d: dict) -> None:
 
 def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> tuple[int, int]:
     """Best (CTA count, division mode) for `params` on the current device
-    (cached)."""
-    import torch
-
+    (cached). Timing is the library's own (fv_time_run: CUDA events around
+    ordinary launches on the handle's stream)."""
     from .solver import Simulation
 
-    device = torch.cuda.get_device_name()
+    device = _abi.device_name()
     key = _key(params, device)
     cache = _load()
     if key in cache and not refresh and "division" in cache[key]:
@@ -58,8 +57,6 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> tuple[int,
     sim = Simulation(params)
     try:
         sim.init_state()
-        stream = torch.cuda.Stream()
-        sim.set_stream(stream.cuda_stream)
         sim.run(10)
         _, resident = sim.get_launch()
         results = {}
@@ -72,14 +69,8 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> tuple[int,
                 except _abi.FvError:
                     continue
                 sim.run(4)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                sim.launch_attempts(steps)
-                e1.record(stream)
-                stream.synchronize()
+                results[(b, mode)] = sim.time_run(steps) / steps
                 sim.sync()
-                results[(b, mode)] = e0.elapsed_time(e1) / steps
         best = min(results, key=results.get)
     finally:
         sim.close()

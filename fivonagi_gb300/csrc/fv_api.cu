@@ -420,6 +420,23 @@ fv_status validate_params(const fv_params *p) { return validate(p); }
 void init_state_host(const fv_params &p, float *u1, float *u2, float *u3) {
   init_host(p, make_dev_params(p), u1, u2, u3);
 }
+
+// One wave of resident CTAs, but no fewer than kMinRowsPerBlock rows per
+// warp (small grids). Every warp of the step kernel streams the same number
+// of rows, so all CTAs of a wave finish together; a second wave would add
+// the warm-up rows of shorter segments, and a partial one (for instance 640
+// CTAs for 608 slots) nearly doubles the time.
+long long default_blocks(int max_resident, long long work) {
+  return std::max(1LL, std::min((long long)max_resident, work / kMinRowsPerBlock));
+}
+
+// Exact division in the step kernel by default. With the normal-quotient
+// division where quotients are normal in practice (DivPair), it is faster
+// than FMA division with its fix-up pass at every size measured: per
+// attempt 0.056 against 0.061 ms at 512x512, 0.096 against 0.109 ms at
+// 1024x1024, 0.144 against 0.165 ms at 2048x1024, 0.447 against 0.498 ms
+// at 4096x2048.
+int default_div_exact(const fv_params &) { return 1; }
 }  // namespace fvgb
 
 namespace {
@@ -512,23 +529,6 @@ fv_status enqueue_attempts(fv_handle *h, long long n) {
     if (rc != 0) return fail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
   }
   return FV_OK;
-}
-
-// One wave of resident CTAs, but no fewer than kMinRowsPerBlock rows per
-// warp (small grids). Every warp of the step kernel streams the same number
-// of rows, so all CTAs of a wave finish together; a second wave would add
-// the warm-up rows of shorter segments, and a partial one (for instance 640
-// CTAs for 608 slots) nearly doubles the time.
-// Exact division in the step kernel by default. With the normal-quotient
-// division where quotients are normal in practice (DivPair), it is faster
-// than FMA division with its fix-up pass at every size measured: per
-// attempt 0.056 against 0.061 ms at 512x512, 0.096 against 0.109 ms at
-// 1024x1024, 0.144 against 0.165 ms at 2048x1024, 0.447 against 0.498 ms
-// at 4096x2048.
-int default_div_exact(const fv_params &) { return 1; }
-
-long long default_blocks(int max_resident, long long work) {
-  return std::max(1LL, std::min((long long)max_resident, work / kMinRowsPerBlock));
 }
 
 fv_status reset_ctrl(fv_handle *h) {
@@ -1075,6 +1075,41 @@ fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_m
   if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "timing events: %s", cudaGetErrorString(ec));
   *step_kernel_ms = float(step_sum / nattempts);
   *attempt_ms = float(att_sum / nattempts);
+  return FV_OK;
+}
+
+fv_status fv_time_run(fv_handle *h, int64_t nattempts, float *ms) {
+  if (!h || nattempts < 1 || !ms) return fail(FV_BAD_ARG, "bad argument");
+  cudaEvent_t ev[2] = {};
+  for (int k = 0; k < 2; ++k) {
+    const cudaError_t e = cudaEventCreate(&ev[k]);
+    if (e != cudaSuccess) {
+      if (k) cudaEventDestroy(ev[0]);
+      return fail(FV_CUDA_ERROR, "cudaEventCreate: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t e = cudaEventRecord(ev[0], h->stream);
+  fv_status s = FV_OK;
+  if (e == cudaSuccess) s = fv_launch_attempts(h, nattempts);
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventRecord(ev[1], h->stream);
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventSynchronize(ev[1]);
+  float t = 0.0f;
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (s != FV_OK) return s;
+  if (e != cudaSuccess) return fail(FV_CUDA_ERROR, "timing events: %s", cudaGetErrorString(e));
+  *ms = t;
+  return FV_OK;
+}
+
+fv_status fv_device_name(char *name, int32_t len) {
+  if (!name || len < 1) return fail(FV_BAD_ARG, "bad argument");
+  int dev = 0;
+  FV_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  FV_CUDA(cudaGetDeviceProperties(&prop, dev));
+  snprintf(name, size_t(len), "%s", prop.name);
   return FV_OK;
 }
 

@@ -368,6 +368,31 @@ fv_status fv_batch_launch_attempts(fv_batch *b, int64_t nattempts) {
   return enqueue_batch(b, nattempts);
 }
 
+fv_status fv_batch_time_run(fv_batch *b, int64_t nattempts, float *ms) {
+  if (!b || nattempts < 1 || !ms) return bfail(FV_BAD_ARG, "bad argument");
+  cudaEvent_t ev[2] = {};
+  for (int k = 0; k < 2; ++k) {
+    const cudaError_t e = cudaEventCreate(&ev[k]);
+    if (e != cudaSuccess) {
+      if (k) cudaEventDestroy(ev[0]);
+      return bfail(FV_CUDA_ERROR, "cudaEventCreate: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t e = cudaEventRecord(ev[0], b->stream);
+  fv_status s = FV_OK;
+  if (e == cudaSuccess) s = fv_batch_launch_attempts(b, nattempts);
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventRecord(ev[1], b->stream);
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventSynchronize(ev[1]);
+  float t = 0.0f;
+  if (e == cudaSuccess && s == FV_OK) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (s != FV_OK) return s;
+  if (e != cudaSuccess) return bfail(FV_CUDA_ERROR, "timing events: %s", cudaGetErrorString(e));
+  *ms = t;
+  return FV_OK;
+}
+
 fv_status fv_batch_sync(fv_batch *b, fv_run_stats *out) {
   if (!b) return bfail(FV_BAD_ARG, "batch is NULL");
   fv_status s = read_batch_ctrl(b);

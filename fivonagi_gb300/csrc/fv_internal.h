@@ -224,6 +224,8 @@ int max_batch_blocks_per_sm_fast();
 // Shared by the C-ABI translation units (fv_api.cu).
 DevParams dev_params_of(const fv_params &p);
 fv_status validate_params(const fv_params *p);
+long long default_blocks(int max_resident, long long work);  // CTAs of a step launch
+int default_div_exact(const fv_params &p);                     // step kernel's division
 void init_state_host(const fv_params &p, float *u1, float *u2, float *u3);
 void set_last_error(const char *msg);
 

@@ -47,7 +47,7 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[FV_NOALLOC_SCRATCH_BYT
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
-int g_max_resident[kMaxDevices] = {};
+int g_max_resident[kMaxDevices][2] = {};  // [device][exact variant]
 int g_sms[kMaxDevices] = {};
 
 // Errors go to the library's per-thread message (fv_last_error_string).
@@ -65,7 +65,7 @@ fv_status nafail(fv_status s, const char *msg, cudaError_t e = cudaSuccess) {
 // and zeroes the fix-up counters and bitmap, so the previous call's
 // contents never leak into this one.
 __global__ void noalloc_begin_kernel(Ctrl *c, uint32_t *fix, int fix_zero_words, float dt, float T,
-                                     int mdx, int mdy, int max_retries) {
+                                     int mdx, int mdy) {
   for (int k = threadIdx.x; k < fix_zero_words; k += blockDim.x) fix[k] = 0u;
   if (threadIdx.x != 0) return;
   c->dt = dt;
@@ -84,7 +84,6 @@ __global__ void noalloc_begin_kernel(Ctrl *c, uint32_t *fix, int fix_zero_words,
   c->accepted = 0;
   c->rejected = 0;
   c->blocks_done = 0u;
-  (void)max_retries;
 }
 
 }  // namespace
@@ -95,19 +94,27 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
                                      int32_t mdy, void *cuda_stream, fv_step_result *res) {
   if (!p || !in_u1 || !in_u2 || !in_u3 || !out_u1 || !out_u2 || !out_u3 || !res)
     return nafail(FV_BAD_ARG, "NULL argument");
-  if (p->app < FV_APP_HIFU_BEAM || p->app > FV_APP_FOCUSED_BEAM)
-    return nafail(FV_BAD_ARG, "unknown app (the phased array needs fv_create's weights)");
-  if (p->nx < 8 || p->ny < 8) return nafail(FV_BAD_ARG, "grid below 8x8");
+  // the checks fv_create makes, then this entry point's own limits
+  const fv_status vs = validate_params(p);
+  if (vs != FV_OK) return vs;
+  if (p->app == FV_APP_PHASED_ARRAY)
+    return nafail(FV_BAD_ARG, "the phased array needs fv_create's weights");
   if ((long long)p->nx + (long long)p->ny > FV_NOALLOC_MAX_PERIMETER)
     return nafail(FV_BAD_ARG, "nx + ny above FV_NOALLOC_MAX_PERIMETER (the ghost frame's room in the scratch array)");
-  if ((long long)p->nx * (long long)p->ny > (1LL << 30)) return nafail(FV_BAD_ARG, "grid above 2^30 cells");
-  if (!(p->xmax > 0) || !(p->ymax > 0) || !(dt > 0)) return nafail(FV_BAD_ARG, "xmax, ymax and dt must be positive");
-  if (p->moving_domain && (p->mdvx < 0 || p->mdvy < 0)) return nafail(FV_BAD_ARG, "mdvx, mdvy must be >= 0");
+  if (!(dt > 0)) return nafail(FV_BAD_ARG, "dt must be positive");
+  // the step kernel streams its input while it writes its output: the two
+  // states must be distinct buffers
+  const float *ins[3] = {in_u1, in_u2, in_u3};
+  const float *outs[3] = {out_u1, out_u2, out_u3};
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      if (ins[a] == outs[b]) return nafail(FV_BAD_ARG, "an output buffer is also an input buffer");
 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return nafail(FV_NO_DEVICE, "cudaGetDevice", e);
   if (dev < 0 || dev >= kMaxDevices) return nafail(FV_NO_DEVICE, "device index out of range");
+  const int variant = p->exact ? 1 : 0;
   unsigned char *base = nullptr;
   int max_resident = 0, sms = 0;
   {
@@ -121,13 +128,14 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
       void *ptr = nullptr;
       e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
       if (e != cudaSuccess || !ptr) return nafail(FV_CUDA_ERROR, "cudaGetSymbolAddress(scratch)", e);
-      const int per_sm = p->exact ? max_blocks_per_sm_exact(4, -1) : max_blocks_per_sm_fast(4, -1);
-      g_max_resident[dev] = per_sm * prop.multiProcessorCount;
+      // resident CTAs of each arithmetic variant's step kernel
+      g_max_resident[dev][0] = max_blocks_per_sm_fast(4, -1) * prop.multiProcessorCount;
+      g_max_resident[dev][1] = max_blocks_per_sm_exact(4, -1) * prop.multiProcessorCount;
       g_sms[dev] = prop.multiProcessorCount;
       g_scratch_addr[dev] = static_cast<unsigned char *>(ptr);
     }
     base = g_scratch_addr[dev];
-    max_resident = g_max_resident[dev];
+    max_resident = g_max_resident[dev][variant];
     sms = g_sms[dev];
   }
 
@@ -136,7 +144,8 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   const int strip_cols = 4 * kWarpCols;
   const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
   const long long work = (long long)nstrips * p->ny;
-  long long blocks = std::max(1LL, std::min(4LL * max_resident, work / 32));
+  // fv_create's launch shape and division
+  long long blocks = default_blocks(max_resident, work);
   if (blocks > kNoallocMaxCtas) blocks = kNoallocMaxCtas;
   const long long windows = (long long)nstrips * 4;
   if (size_t(fix_scratch_words(windows, p->ny)) * sizeof(uint32_t) > kFixBytes)
@@ -160,11 +169,11 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   a.nblocks = int(blocks);
   a.work = work;
   a.fix_blocks = std::min(kNoallocMaxFixCtas, std::max(1, 4 * sms));
+  a.div_exact = default_div_exact(*p);
 
   cudaStream_t st = (cudaStream_t)cuda_stream;
   const int fix_zero_words = int(4 + fix_bitmap_words(windows, p->ny));
-  noalloc_begin_kernel<<<1, 256, 0, st>>>(ctrl, fix, fix_zero_words, float(dt), float(T), mdx, mdy,
-                                          a.p.max_retries);
+  noalloc_begin_kernel<<<1, 256, 0, st>>>(ctrl, fix, fix_zero_words, float(dt), float(T), mdx, mdy);
   e = cudaGetLastError();
   if (e != cudaSuccess) return nafail(FV_CUDA_ERROR, "control-block launch", e);
   const int rc = p->exact ? launch_step_exact(a, 4, -1, st) : launch_step_fast(a, 4, -1, st);

@@ -190,6 +190,13 @@ class Simulation:
         check(self.lib.fv_time_attempts(self.h, int(n), C.byref(sk), C.byref(at)), "fv_time_attempts")
         return sk.value, at.value
 
+    def time_run(self, n: int) -> float:
+        """Device ms of n attempts launched as launch_attempts does (CUDA
+        events on the handle's stream; fv_time_run). Synchronises."""
+        ms = C.c_float()
+        check(self.lib.fv_time_run(self.h, int(n), C.byref(ms)), "fv_time_run")
+        return ms.value
+
     def sync(self) -> dict:
         st = FvRunStats()
         check(self.lib.fv_sync(self.h, C.byref(st)), "fv_sync")
@@ -282,6 +289,13 @@ class Batch:
 
     def launch_attempts(self, n: int) -> None:
         check(self.lib.fv_batch_launch_attempts(self.h, int(n)), "fv_batch_launch_attempts")
+
+    def time_run(self, n: int) -> float:
+        """Device ms of n attempts of every simulation, launched as
+        launch_attempts does (fv_batch_time_run). Synchronises."""
+        ms = C.c_float()
+        check(self.lib.fv_batch_time_run(self.h, int(n), C.byref(ms)), "fv_batch_time_run")
+        return ms.value
 
     def sync(self) -> list[dict]:
         st = (FvRunStats * self.n)()

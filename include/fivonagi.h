@@ -283,6 +283,17 @@ fv_status fv_sync(fv_handle *h, fv_run_stats *out);
 fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_ms,
                            float *attempt_ms);
 
+/* Enqueues nattempts attempts as fv_launch_attempts does, between two
+ * CUDA events on the handle's stream, synchronises, and returns the elapsed
+ * device time in ms (the counters cover those attempts, as after
+ * fv_launch_attempts; read them with fv_sync). For the autotuner. No
+ * reference counterpart. */
+fv_status fv_time_run(fv_handle *h, int64_t nattempts, float *ms);
+
+/* Name of the current CUDA device (cudaGetDeviceProperties), NUL-terminated
+ * within len bytes; the autotuner's cache key. No reference counterpart. */
+fv_status fv_device_name(char *name, int32_t len);
+
 /* Launch shape of the step kernel, for the autotuner: `blocks` persistent
  * CTAs of 4 warps, each warp streaming an even share of the grid's
  * (26-column window, row) work; 0 restores the default (one wave of
@@ -341,6 +352,9 @@ fv_status fv_batch_run(fv_batch *b, int64_t nsteps, fv_run_stats *out);
  * fv_batch_sync waits and reports. */
 fv_status fv_batch_launch_attempts(fv_batch *b, int64_t nattempts);
 fv_status fv_batch_sync(fv_batch *b, fv_run_stats *out);
+/* fv_batch_launch_attempts between two CUDA events on the batch's stream;
+ * synchronises and returns the elapsed device time in ms. */
+fv_status fv_batch_time_run(fv_batch *b, int64_t nattempts, float *ms);
 /* CTAs of the batch launch, each warp streaming an even share of the
  * concatenated (simulation, window, row) work (0 = default: eight waves of
  * resident CTAs, at least 32 rows per warp). */
@@ -362,8 +376,14 @@ fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_residen
  * are rejected with FV_BAD_ARG. All calls on a device share the array, so
  * calls that overlap on the GPU race: serialise them. The first call on
  * each device looks up the array's address, so make it before any stream
- * capture. res->accepted = 0 means CFL >= CFLMAX: retry from the same input
- * with res->dt_next. No reference counterpart. */
+ * capture. The input and output buffers must be distinct (FV_BAD_ARG
+ * otherwise). The attempt runs fv_create's launch shape and division.
+ * Each call is one attempt: res->accepted = 0 means CFL >= CFLMAX, the
+ * output holds no step, and res->dt_next is the retry's dt (update_dt's 0.9
+ * rule); retry from the same input with it. The library keeps no count of
+ * rejections across calls, so the caller bounds its own retries
+ * (res->status is FV_DT_TOO_LARGE after a rejection only when
+ * p->max_retries is 1). No reference counterpart. */
 #define FV_NOALLOC_SCRATCH_BYTES (2104u * 1024u)
 #define FV_NOALLOC_MAX_CTAS 2048
 #define FV_NOALLOC_MAX_PERIMETER 16384

@@ -23,7 +23,8 @@ from fivonagi_gb300._abi import FvParams, FvRunStats
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libfvref.so")
-REF_ROOT_DEFAULT = "/root/reference"
+# where the reference source tree is, for the host build of its headers
+REF_ROOT_ENV = "FIVONAGI_REF_ROOT"
 
 REF_APP_KEYS = {0: "hifu", 1: "taylor", 2: "plane", 3: "focused"}
 
@@ -32,10 +33,12 @@ _ref = None
 
 
 def build_oracle(ref_root: str | None = None, with_ref: bool = True) -> None:
-    """Compile the restatement, and the reference shim when its tree exists."""
+    """Compile the restatement, and the reference shim when a reference tree
+    is given (`ref_root`, or the FIVONAGI_REF_ROOT environment variable) and
+    exists."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    root = ref_root or REF_ROOT_DEFAULT
-    if with_ref and os.path.isdir(os.path.join(root, "apps", "na")):
+    root = ref_root or os.environ.get(REF_ROOT_ENV)
+    if with_ref and root and os.path.isdir(os.path.join(root, "apps", "na")):
         subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF_ROOT={root}"], check=True)
 
 

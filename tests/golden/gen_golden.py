@@ -12,7 +12,8 @@ in FP32 and FP64, and stores what it produced:
 
 Inputs are reproducible without the reference: the init hook's output plus
 a numpy default_rng(seed) perturbation, both recorded. Run from the repo
-root: python tests/golden/gen_golden.py  (needs the reference tree).
+root: python tests/golden/gen_golden.py [reference tree]  (the tree defaults
+to FIVONAGI_REF_ROOT, else /root/reference, where this image mounts it).
 """
 from __future__ import annotations
 
@@ -61,7 +62,8 @@ def cases_small():
 
 def main():
     if not oracle.ref_available():
-        oracle.build_oracle()
+        tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(oracle.REF_ROOT_ENV, "/root/reference")
+        oracle.build_oracle(ref_root=tree)
     arrays = {}
     meta = {"small": [], "hashed": []}
     # ---- 32x16: full grids
