@@ -387,14 +387,13 @@ def error_report(params, nsteps: int) -> dict:
     }
 
 
-def time_plain(params, blocks, division, steps, warmup, stream=None, sampler=None):
+def time_plain(params, launch, steps, warmup, stream=None, sampler=None):
     """Device time of `steps` back-to-back attempts of the headline workload
-    (CUDA events on the handle's stream)."""
-    from fivonagi_gb300 import Simulation
+    (CUDA events on the handle's stream) with the launch `launch`."""
+    from fivonagi_gb300 import Simulation, autotune
 
     sim = Simulation(params)
-    sim.set_launch(blocks)
-    sim.set_division(division)
+    autotune.set_launch(sim, launch)
     sim.init_state()
     if stream is not None:
         sim.set_stream(stream)
@@ -414,8 +413,8 @@ def fast_report(args, cells) -> dict:
     from fivonagi_gb300 import autotune
 
     p = headline_params(exact=False)
-    blocks, division = autotune.tune(p)
-    sim, ms, st = time_plain(p, blocks, division, args.steps, args.warmup)
+    launch = autotune.tune(p)
+    sim, ms, st = time_plain(p, launch, args.steps, args.warmup)
     sim.close()
     return {"value": cells * st["accepted"] / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
             "ms_per_step": ms / max(1, st["accepted"]), "steps": args.steps,
@@ -440,10 +439,9 @@ def batched_report(args) -> dict:
     batched = sum(c * a for c, a in zip(cells, acc)) / (ms_batch * 1e-3) / 1e9
     ms_seq, work_seq = 0.0, 0
     for p in plist:
-        blocks, division = autotune.tune(p, steps=20)
+        launch = autotune.tune(p, steps=20)
         sim = Simulation(p)
-        sim.set_launch(blocks)
-        sim.set_division(division)
+        autotune.set_launch(sim, launch)
         sim.init_state()
         sim.run(max(args.warmup, 3))
         ms_seq += sim.time_run(args.steps)
@@ -506,11 +504,13 @@ def run_gpu(args):
     # profiler's capture)
     DIVISIONS = {"default": _abi.FV_DIVISION_DEFAULT, "fma": _abi.FV_DIVISION_FMA, "exact": _abi.FV_DIVISION_EXACT}
     if args.blocks > 0:
-        blocks, division = args.blocks, DIVISIONS[args.division]
+        launch = autotune.Launch(args.blocks, DIVISIONS[args.division], max(args.shape, 0))
     else:
-        blocks, division = autotune.tune(params)
+        launch = autotune.tune(params)
         if args.division != "default":
-            division = DIVISIONS[args.division]
+            launch = launch._replace(division=DIVISIONS[args.division])
+        if args.shape >= 0:
+            launch = launch._replace(shape=args.shape)
 
     # ---- device-timed throughput (state resident in HBM): K back-to-back
     # attempts between CUDA events on the solver's stream
@@ -518,7 +518,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    sim, ms, st = time_plain(params, blocks, division, args.steps, args.warmup, stream.cuda_stream, sampler)
+    sim, ms, st = time_plain(params, launch, args.steps, args.warmup, stream.cuda_stream, sampler)
     division_used = "exact" if sim.get_division() == _abi.FV_DIVISION_EXACT else "fma"
     if world > 1:
         torch.distributed.barrier()
@@ -548,8 +548,7 @@ def run_gpu(args):
 
     # ---- end to end through the C ABI with pinned host buffers
     sim = Simulation(params)
-    sim.set_launch(blocks)
-    sim.set_division(division)
+    autotune.set_launch(sim, launch)
     sim.set_stream(stream.cuda_stream)
     u0 = torch.zeros((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
     u_out = torch.empty((3, params.ny, params.nx), dtype=torch.float32, pin_memory=True)
@@ -625,7 +624,8 @@ def run_gpu(args):
             "variant": "exact (no FMA contraction; bit-identical to the oracle)" if exact else "fast (FMA)",
             "accepted": accepted, "rejected": int(st["rejected"]), "T_end": st["T"],
             "parallelism": "replicas" if world > 1 else "single GPU",
-            "ctas_per_launch": blocks, "step_division": division_used,
+            "ctas_per_launch": launch.blocks, "step_division": division_used,
+            "cta_shape": _abi.FV_CTA_SHAPES[launch.shape] + " (warps per CTA x CTAs per SM)",
             "attempt_ms_l2_flushed": flushed_ms,
         },
         "roofline": roofline,
@@ -909,6 +909,9 @@ def main():
                          "case for a profiler's launch list)")
     ap.add_argument("--blocks", type=int, default=0,
                     help="plain workload: CTAs per step launch instead of the autotuner's choice")
+    ap.add_argument("--shape", type=int, default=-1, choices=[-1, *range(4)],
+                    help="plain workload: the step kernel's CTA shape (fv_set_cta_shape) instead of the "
+                         "autotuner's (or, with --blocks, shape 0)")
     ap.add_argument("--division", choices=["default", "fma", "exact"], default="default",
                     help="plain workload: the step kernel's division instead of the autotuner's (or, with "
                          "--blocks, the library default's) choice")

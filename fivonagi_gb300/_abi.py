@@ -43,6 +43,9 @@ FV_APP_PLANE_WAVE = 2
 FV_APP_FOCUSED_BEAM = 3
 FV_APP_PHASED_ARRAY = 4
 
+# CTA shapes of the step kernel (fv_set_cta_shape): warps per CTA x CTAs per SM
+FV_CTA_SHAPES = {0: "4x4", 1: "2x8", 2: "1x16", 3: "1x18"}
+
 # division in the step kernel (fv_set_division)
 FV_DIVISION_DEFAULT = -1
 FV_DIVISION_FMA = 0
@@ -222,6 +225,8 @@ PROTOTYPES = {
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "fv_set_launch": (C.c_int, [_P, C.c_int32]),
+    "fv_set_cta_shape": (C.c_int, [_P, C.c_int32]),
+    "fv_get_cta_shape": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "fv_get_launch": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "fv_batch_create": (C.c_int, [C.c_int32, C.POINTER(FvParams), C.POINTER(_P)]),
     "fv_batch_destroy": (C.c_int, [_P]),

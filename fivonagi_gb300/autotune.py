@@ -1,30 +1,44 @@
 """Launch-shape autotuner for the step kernel.
 
-The step kernel has two free launch parameters: the number of persistent
-CTAs whose warps share the grid's (window, row) work (fv_set_launch), and
-the division it computes with (fv_set_division: FMA division with a fix-up
-pass, or exact division with no fix-up work; the results are the same bit
-for bit). More waves keep every SM full to the end but repeat the streaming
-loop's warm-up rows on shorter segments; exact division costs the step
-kernel a few percent and saves the fix-up pass. The best pair depends on
-the grid size. `tune` times each pair, in waves of the CTAs resident at
-once, on a scratch copy of the simulation, and caches the winner per
-(device, grid, variant) in a JSON file next to the library.
+The step kernel has three free launch parameters, none of which changes its
+results (every warp streams its own share of the grid's (window, row) work
+with the same arithmetic):
+  * the CTA shape (fv_set_cta_shape): warps per CTA and the CTAs per SM the
+    kernel is built for -- 4 x 4, 2 x 8, 1 x 16, or 1 x 18 with a smaller
+    register budget and more warps per SM;
+  * the number of persistent CTAs (fv_set_launch), in waves of the CTAs
+    resident at once: more waves keep every SM full to the end but repeat
+    the streaming loop's warm-up rows on shorter segments;
+  * the division (fv_set_division): FMA division with a fix-up pass, or
+    exact division with no fix-up work (FMA division runs shape 0 only).
+The best choice depends on the grid size. `tune` times each candidate on a
+scratch copy of the simulation with the library's own CUDA-event timing
+(fv_time_run) and caches the winner per (device, grid, variant) in a JSON
+file next to the library.
 """
 from __future__ import annotations
 
 import json
 import os
+from typing import NamedTuple
 
 from . import _abi
 from ._abi import FvParams
 
 CACHE = os.path.join(_abi.LIB_DIR, "autotune.json")
+CACHE_VERSION = 2
 WAVES = (1, 2, 3, 4, 6, 8)
+SHAPES = tuple(_abi.FV_CTA_SHAPES)
+
+
+class Launch(NamedTuple):
+    blocks: int
+    division: int
+    shape: int
 
 
 def _key(params: FvParams, device: str) -> str:
-    return f"{device}|{params.nx}x{params.ny}|exact={params.exact}"
+    return f"v{CACHE_VERSION}|{device}|{params.nx}x{params.ny}|exact={params.exact}"
 
 
 def _load() -> dict:
@@ -43,47 +57,62 @@ def _store(d: dict) -> None:
     os.replace(tmp, CACHE)
 
 
-def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> tuple[int, int]:
-    """Best (CTA count, division mode) for `params` on the current device
-    (cached). Timing is the library's own (fv_time_run: CUDA events around
-    ordinary launches on the handle's stream)."""
+def candidates():
+    """(shape, division) pairs: every shape with exact division, shape 0
+    with FMA division."""
+    for shape in SHAPES:
+        yield shape, _abi.FV_DIVISION_EXACT
+    yield 0, _abi.FV_DIVISION_FMA
+
+
+def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> Launch:
+    """Best launch for `params` on the current device (cached)."""
     from .solver import Simulation
 
     device = _abi.device_name()
     key = _key(params, device)
     cache = _load()
-    if key in cache and not refresh and "division" in cache[key]:
-        return int(cache[key]["blocks"]), int(cache[key]["division"])
+    if key in cache and not refresh:
+        c = cache[key]
+        return Launch(int(c["blocks"]), int(c["division"]), int(c["shape"]))
     sim = Simulation(params)
+    results = {}
     try:
         sim.init_state()
         sim.run(10)
-        _, resident = sim.get_launch()
-        results = {}
-        for mode in (_abi.FV_DIVISION_FMA, _abi.FV_DIVISION_EXACT):
+        for shape, mode in candidates():
             sim.set_division(mode)
+            sim.set_cta_shape(shape)
+            _, resident = sim.get_launch()
             for w in WAVES:
-                b = w * resident
                 try:
-                    sim.set_launch(b)
+                    sim.set_launch(w * resident)
                 except _abi.FvError:
                     continue
                 sim.run(4)
-                results[(b, mode)] = sim.time_run(steps) / steps
+                results[Launch(w * resident, mode, shape)] = sim.time_run(steps) / steps
                 sim.sync()
         best = min(results, key=results.get)
     finally:
         sim.close()
-    cache[key] = {"blocks": best[0], "division": best[1], "ms_per_step": results[best],
-                  "candidates": {f"{b}/{'exact' if m else 'fma'}": v for (b, m), v in sorted(results.items())}}
+    cache[key] = {"blocks": best.blocks, "division": best.division, "shape": best.shape,
+                  "ms_per_step": results[best],
+                  "candidates": {f"{_abi.FV_CTA_SHAPES[c.shape]}/{c.blocks}/{'exact' if c.division else 'fma'}": v
+                                 for c, v in sorted(results.items())}}
     _store(cache)
     return best
 
 
-def apply(sim, refresh: bool = False) -> tuple[int, int]:
-    """Tune for `sim`'s parameters and set its launch shape and division;
-    returns (CTAs, division mode)."""
-    b, m = tune(sim.params, refresh=refresh)
-    sim.set_launch(b)
-    sim.set_division(m)
-    return b, m
+def apply(sim, refresh: bool = False) -> Launch:
+    """Tune for `sim`'s parameters and set its CTA shape, launch and
+    division; returns the choice."""
+    best = tune(sim.params, refresh=refresh)
+    set_launch(sim, best)
+    return best
+
+
+def set_launch(sim, launch: Launch) -> None:
+    """Put `launch` on a Simulation (division, shape, then CTAs)."""
+    sim.set_division(launch.division)
+    sim.set_cta_shape(launch.shape)
+    sim.set_launch(launch.blocks)

@@ -294,8 +294,12 @@ struct fv_handle {
   StepArgs args{};
   int warps = 4;
   bool exact = true;
-  int max_resident = 0;       // CTAs that fit on the device at once
+  int max_resident = 0;       // CTAs of the current step launch that fit on the device at once
   int partials_cap = 0;       // capacity of `partials`
+  int sms = 0;
+  int fma_resident = 0;                  // resident CTAs of the FMA-division step kernel
+  int shape_resident[kStepShapes] = {};  // ... of the exact-division kernel in each CTA shape
+  int shape_warps[kStepShapes] = {};     // warps per CTA of each shape
 };
 
 namespace {
@@ -304,6 +308,9 @@ int launch(fv_handle *h, int stage, const StepArgs &a) {
   return h->exact ? launch_step_exact(a, h->warps, stage, h->stream)
                   : launch_step_fast(a, h->warps, stage, h->stream);
 }
+
+// warps per CTA of the attempts' step launch
+int step_cta_warps(const fv_handle *h) { return h->args.div_exact ? h->shape_warps[h->args.shape] : 4; }
 
 // One attempt of the run: the step's launches, then the collector if on.
 int launch_attempt(fv_handle *h) {
@@ -426,8 +433,10 @@ void init_state_host(const fv_params &p, float *u1, float *u2, float *u3) {
 // of rows, so all CTAs of a wave finish together; a second wave would add
 // the warm-up rows of shorter segments, and a partial one (for instance 640
 // CTAs for 608 slots) nearly doubles the time.
-long long default_blocks(int max_resident, long long work) {
-  return std::max(1LL, std::min((long long)max_resident, work / kMinRowsPerBlock));
+long long default_blocks(int max_resident, long long work, int cta_warps) {
+  // work counts rows of 4-window strips: kMinRowsPerBlock rows per warp
+  const long long most = work * 4 / ((long long)std::max(cta_warps, 1) * kMinRowsPerBlock);
+  return std::max(1LL, std::min((long long)max_resident, most));
 }
 
 // Exact division in the step kernel by default. With the normal-quotient
@@ -730,10 +739,20 @@ fv_status fv_create(const fv_params *p, fv_handle **out) {
   const int strip_cols = h->warps * kWarpCols;
   const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
   const long long work = (long long)nstrips * p->ny;
+  h->sms = prop.multiProcessorCount;
   const int per_sm = h->exact ? max_blocks_per_sm_exact(h->warps, -1) : max_blocks_per_sm_fast(h->warps, -1);
-  h->max_resident = per_sm * prop.multiProcessorCount;
-  long long blocks = default_blocks(h->max_resident, work);
-  h->partials_cap = std::max(h->max_resident, 1) * 8;
+  h->fma_resident = per_sm * prop.multiProcessorCount;
+  int most_resident = h->fma_resident;
+  for (int k = 0; k < kStepShapes; ++k) {
+    int w = 4;
+    const int nb = h->exact ? step_shape_blocks_per_sm_exact(k, &w) : step_shape_blocks_per_sm_fast(k, &w);
+    h->shape_resident[k] = nb * prop.multiProcessorCount;
+    h->shape_warps[k] = w;
+    most_resident = std::max(most_resident, h->shape_resident[k]);
+  }
+  h->max_resident = default_div_exact(*p) ? h->shape_resident[0] : h->fma_resident;
+  long long blocks = default_blocks(h->max_resident, work, 4);
+  h->partials_cap = std::max(most_resident, 1) * 8;
   // the fix-up launch: four CTAs per SM (two waves at its occupancy of two);
   // warp w takes marked items w, w + W, ..., so warps past the last item exit
   // at once
@@ -1181,7 +1200,7 @@ fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out) {
 
 fv_status fv_set_launch(fv_handle *h, int32_t blocks) {
   if (!h || blocks < 0) return fail(FV_BAD_ARG, "bad argument");
-  const long long b = blocks == 0 ? default_blocks(h->max_resident, h->args.work) : blocks;
+  const long long b = blocks == 0 ? default_blocks(h->max_resident, h->args.work, step_cta_warps(h)) : blocks;
   if (b > h->partials_cap) return fail(FV_BAD_ARG, "blocks %lld above %d", b, h->partials_cap);
   FV_CUDA(cudaStreamSynchronize(h->stream));
   h->args.nblocks = int(b);
@@ -1200,7 +1219,25 @@ fv_status fv_set_division(fv_handle *h, int32_t mode) {
   if (!h || mode < FV_DIVISION_DEFAULT || mode > FV_DIVISION_EXACT) return fail(FV_BAD_ARG, "bad argument");
   FV_CUDA(cudaStreamSynchronize(h->stream));
   h->args.div_exact = mode == FV_DIVISION_DEFAULT ? default_div_exact(h->params) : (mode == FV_DIVISION_EXACT);
+  h->max_resident = h->args.div_exact ? h->shape_resident[h->args.shape] : h->fma_resident;
   drop_graphs(h);
+  return FV_OK;
+}
+
+fv_status fv_set_cta_shape(fv_handle *h, int32_t shape) {
+  if (!h || shape < 0 || shape >= kStepShapes) return fail(FV_BAD_ARG, "bad argument");
+  FV_CUDA(cudaStreamSynchronize(h->stream));
+  h->args.shape = shape;
+  h->max_resident = h->args.div_exact ? h->shape_resident[shape] : h->fma_resident;
+  h->args.nblocks = int(default_blocks(h->max_resident, h->args.work, step_cta_warps(h)));
+  drop_graphs(h);
+  return FV_OK;
+}
+
+fv_status fv_get_cta_shape(fv_handle *h, int32_t *shape, int32_t *warps_per_cta) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (shape) *shape = h->args.shape;
+  if (warps_per_cta) *warps_per_cta = step_cta_warps(h);
   return FV_OK;
 }
 

@@ -177,7 +177,14 @@ struct StepArgs {
   int32_t fix_blocks;     // CTAs of the fix-up launch
   int32_t div_exact;      // attempts (-1, kLaunchStep) run the step kernel with exact
                           // division (kStageExactDiv) instead of FMA division
+  int32_t shape;          // CTA shape of the exact-division step kernel (kStepShapes)
 };
+
+// CTA shapes of the exact-division step kernel: {warps per CTA, CTAs per
+// SM it is built for}. 0: 4 x 4 (16 warps per SM), 1: 2 x 8, 2: 1 x 16,
+// 3: 1 x 18 (18 warps per SM, at most 112 registers a thread). The
+// FMA-division and stage-recording kernels run shape 0.
+constexpr int kStepShapes = 4;
 
 // One simulation of a batch: its parameters, buffers and control block,
 // and where its window-rows start in the batch's concatenated work.
@@ -216,6 +223,9 @@ int launch_step_exact(const StepArgs &a, int warps, int stage, void *stream);
 int launch_step_fast(const StepArgs &a, int warps, int stage, void *stream);
 int max_blocks_per_sm_exact(int warps, int stage);
 int max_blocks_per_sm_fast(int warps, int stage);
+// CTAs per SM of the exact-division step kernel in a CTA shape, and its warps per CTA
+int step_shape_blocks_per_sm_exact(int shape, int *warps);
+int step_shape_blocks_per_sm_fast(int shape, int *warps);
 int launch_batch_exact(const BatchArgs &a, void *stream);
 int launch_batch_fast(const BatchArgs &a, void *stream);
 int max_batch_blocks_per_sm_exact();
@@ -224,7 +234,7 @@ int max_batch_blocks_per_sm_fast();
 // Shared by the C-ABI translation units (fv_api.cu).
 DevParams dev_params_of(const fv_params &p);
 fv_status validate_params(const fv_params *p);
-long long default_blocks(int max_resident, long long work);  // CTAs of a step launch
+long long default_blocks(int max_resident, long long work, int cta_warps);  // CTAs of a step launch
 int default_div_exact(const fv_params &p);                     // step kernel's division
 void init_state_host(const fv_params &p, float *u1, float *u2, float *u3);
 void set_last_error(const char *msg);

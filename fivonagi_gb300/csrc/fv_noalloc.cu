@@ -145,7 +145,7 @@ extern "C" fv_status fv_step_noalloc(const fv_params *p, const float *in_u1, con
   const int nstrips = (p->nx + strip_cols - 1) / strip_cols;
   const long long work = (long long)nstrips * p->ny;
   // fv_create's launch shape and division
-  long long blocks = default_blocks(max_resident, work);
+  long long blocks = default_blocks(max_resident, work, 4);
   if (blocks > kNoallocMaxCtas) blocks = kNoallocMaxCtas;
   const long long windows = (long long)nstrips * 4;
   if (size_t(fix_scratch_words(windows, p->ny)) * sizeof(uint32_t) > kFixBytes)

@@ -275,7 +275,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       // normal = u3: the normal velocity's quotients are the others (DivPair)
       yo.ok = riemann<true, DP::kSubsonic>(rho, u.u3, u.u2, yo.vy, yo.vx, s0_m1.u1 + 1.0f, s0_m1.u3, s0_m1.u2, vy_m1,
                             vx_m1, two_bm1, dty, yo.cy, yo.w, yo.f, dp.s, dp.x);
-      yo.dr = wave_dots(w_m1, yo.w);
+      yo.dr = wave_dots<DP::kSubsonic>(w_m1, yo.w);
       correction<DP::kSubsonic>(w_m1, dl_m1, yo.dr, dty, yo.fa1, yo.fa2, yo.fa3, dp.s);
     };
     auto x_chain = [&](auto &dp) {
@@ -295,7 +295,7 @@ __device__ __forceinline__ void stream_strip(const DevParams &p, const float *co
       wn.w11 = shdn(wx.w11); wn.w21 = shdn(wx.w21); wn.w31 = shdn(wx.w31);
       wn.w12 = shdn(wx.w12); wn.w22 = shdn(wx.w22); wn.w32 = shdn(wx.w32);
       wn.w33 = shdn(wx.w33);
-      const Dots drx = wave_dots(wx, wn);
+      const Dots drx = wave_dots<DP::kSubsonic>(wx, wn);
       Dots dlx;
       dlx.d1 = shup(drx.d1); dlx.d2 = shup(drx.d2); dlx.d3 = shup(drx.d3);
       float fx1, fx2, fx3;
@@ -560,6 +560,7 @@ __device__ __forceinline__ void stream_window(const DevParams &p, const float *c
 
 // The CTA's CFL maximum into partials[slot], and the negative-eigenvalue
 // flag into the control block.
+template <int W = kWarps>
 __device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg, int slot, float *red,
                                         int *sh) {
   const int warp = threadIdx.x >> 5;
@@ -571,7 +572,7 @@ __device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg,
   __syncthreads();
   if (threadIdx.x == 0) {
     float m = red[0];
-    for (int w = 1; w < kWarps; ++w) m = nanmax(m, red[w]);
+    for (int w = 1; w < W; ++w) m = nanmax(m, red[w]);
     a.partials[slot] = m;
     if (sh[0]) ((volatile Ctrl *)a.ctrl)->neg_flag = 1;
   }
@@ -580,10 +581,13 @@ __device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg,
 // The step: STAGE < 0 is the full attempt with FMA division, followed by
 // the fix-up and finalize launches (kStageRecord also writes the stage
 // grids); STAGE 0..3 write that stage's grid to the debug buffers with IEEE
-// division.
-template <int STAGE>
-__global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
-  __shared__ float red[kWarps];
+// division. W warps per CTA, built for MINB CTAs per SM (the register
+// budget): the CTA shape (StepArgs::shape) only changes how the launch's
+// warps are grouped and how many fit on an SM; every warp streams its own
+// share either way.
+template <int STAGE, int W>
+__device__ __forceinline__ void step_body(const StepArgs &a) {
+  __shared__ float red[W];
   __shared__ int sh[1];
   const Ctrl *ctl = a.ctrl;
   // Uniform early exit: the control block only changes between launches.
@@ -620,8 +624,8 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
   // launch's cost (ShareCost).
   const ShareCost sc(a.p.nx, ny);
   const long long C = sc.total();
-  const long long G = (long long)a.nblocks * kWarps;
-  const long long g = (long long)blockIdx.x * kWarps + warp;
+  const long long G = (long long)a.nblocks * W;
+  const long long g = (long long)blockIdx.x * W + warp;
   const long long s0 = sc.pos(g * C / G), s1 = sc.pos((g + 1) * C / G);
   for (long long pos = s0; pos < s1;) {
     const int win = (int)(pos / ny);
@@ -639,7 +643,40 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel(StepArgs a) {
     pos += y1 - y0;
   }
   if (STAGE >= 0) return;
-  publish(a, cmax, neg, blockIdx.x, red, sh);
+  publish<W>(a, cmax, neg, blockIdx.x, red, sh);
+}
+
+template <int STAGE, int W = kWarps, int MINB = 4>
+__global__ void __launch_bounds__(W * kLanes, MINB) step_kernel(StepArgs a) {
+  step_body<STAGE, W>(a);
+}
+
+// One-warp CTAs with a register cap (__maxnreg__ cannot join
+// __launch_bounds__): MAXREG registers a thread hold 65536 / (32 MAXREG)
+// warps per SM.
+template <int STAGE, int MAXREG>
+__global__ void __maxnreg__(MAXREG) step_kernel_r(StepArgs a) {
+  step_body<STAGE, 1>(a);
+}
+
+// The exact-division step kernel in the CTA shape `shape` (kStepShapes):
+// warps per CTA and the CTAs per SM it is built for.
+static void *exact_step_ptr(int shape, int &threads) {
+  switch (shape) {
+    case 1: threads = 2 * kLanes; return (void *)step_kernel<kStageExactDiv, 2, 8>;
+    case 2: threads = kLanes; return (void *)step_kernel_r<kStageExactDiv, 128>;
+    case 3: threads = kLanes; return (void *)step_kernel_r<kStageExactDiv, 112>;
+    default: threads = kThreads; return (void *)step_kernel<kStageExactDiv, kWarps, 4>;
+  }
+}
+
+static void launch_exact_step(const StepArgs &a, cudaStream_t st) {
+  switch (a.shape) {
+    case 1: step_kernel<kStageExactDiv, 2, 8><<<a.nblocks, 2 * kLanes, 0, st>>>(a); break;
+    case 2: step_kernel_r<kStageExactDiv, 128><<<a.nblocks, kLanes, 0, st>>>(a); break;
+    case 3: step_kernel_r<kStageExactDiv, 112><<<a.nblocks, kLanes, 0, st>>>(a); break;
+    default: step_kernel<kStageExactDiv><<<a.nblocks, kThreads, 0, st>>>(a); break;
+  }
 }
 
 // Recomputes the chunks the step launch marked, with exact division
@@ -990,7 +1027,7 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
     case kLaunchFrame: break;
     case kLaunchStep:
       if (a.div_exact)
-        step_kernel<kStageExactDiv><<<grid, block, 0, st>>>(a);
+        launch_exact_step(a, st);
       else
         step_kernel<-1><<<grid, block, 0, st>>>(a);
       break;
@@ -1000,7 +1037,7 @@ static int launch_impl(const StepArgs &a, int stage, void *stream) {
       break;
     case -1:
       if (a.div_exact)
-        step_kernel<kStageExactDiv><<<grid, block, 0, st>>>(a);
+        launch_exact_step(a, st);
       else
         step_kernel<-1><<<grid, block, 0, st>>>(a);
       fixup_kernel<-1><<<a.fix_blocks, block, 0, st>>>(a);
@@ -1028,6 +1065,15 @@ static int occupancy(int stage) {
   return nb > 0 ? nb : 1;
 }
 
+// CTAs per SM of the exact-division step kernel in CTA shape `shape`.
+static int shape_occupancy(int shape, int &warps) {
+  int threads = 0, nb = 0;
+  void *k = exact_step_ptr(shape, threads);
+  warps = threads / kLanes;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, 0) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
 }  // namespace exact_ns / fast_ns
 
 #if FV_VARIANT_EXACT
@@ -1040,6 +1086,7 @@ int launch_step_exact(const StepArgs &a, int warps, int stage, void *stream) {
 int max_blocks_per_sm_exact(int warps, int stage) {
   return warps == exact_ns::kWarps ? exact_ns::occupancy(stage) : 0;
 }
+int step_shape_blocks_per_sm_exact(int shape, int *warps) { return exact_ns::shape_occupancy(shape, *warps); }
 #else
 int launch_batch_fast(const BatchArgs &a, void *stream) { return fast_ns::launch_batch_impl(a, stream); }
 int max_batch_blocks_per_sm_fast() { return fast_ns::batch_occupancy(); }
@@ -1050,6 +1097,7 @@ int launch_step_fast(const StepArgs &a, int warps, int stage, void *stream) {
 int max_blocks_per_sm_fast(int warps, int stage) {
   return warps == fast_ns::kWarps ? fast_ns::occupancy(stage) : 0;
 }
+int step_shape_blocks_per_sm_fast(int shape, int *warps) { return fast_ns::shape_occupancy(shape, *warps); }
 #endif
 
 }  // namespace fvgb

@@ -212,6 +212,17 @@ class Simulation:
         check(self.lib.fv_get_launch(self.h, C.byref(b), C.byref(m)), "fv_get_launch")
         return b.value, m.value
 
+    def set_cta_shape(self, shape: int) -> None:
+        """The step kernel's CTA shape (fv_set_cta_shape); resets the CTA
+        count to the shape's default."""
+        check(self.lib.fv_set_cta_shape(self.h, int(shape)), "fv_set_cta_shape")
+
+    def get_cta_shape(self) -> tuple[int, int]:
+        """(shape, warps per CTA) of the step kernel."""
+        s, w = C.c_int32(), C.c_int32()
+        check(self.lib.fv_get_cta_shape(self.h, C.byref(s), C.byref(w)), "fv_get_cta_shape")
+        return s.value, w.value
+
     def set_division(self, mode: int) -> None:
         """Division in the step kernel (fv_set_division): _abi.FV_DIVISION_FMA,
         FV_DIVISION_EXACT or FV_DIVISION_DEFAULT; results are the same."""

@@ -303,6 +303,18 @@ fv_status fv_device_name(char *name, int32_t len);
 fv_status fv_set_launch(fv_handle *h, int32_t blocks);
 fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident);
 
+/* CTA shape of the step kernel, for the autotuner: 0 = 4 warps per CTA,
+ * 4 CTAs per SM (the default); 1 = 2 warps, 8 per SM; 2 = 1 warp, 16 per
+ * SM; 3 = 1 warp, 18 per SM (built for at most 112 registers a thread).
+ * Every warp streams its own share of the grid in every shape, so the
+ * results are the same bit for bit; what changes is how many warps an SM
+ * holds and how the launch groups them. Applies to the exact-division
+ * kernel (FMA division runs shape 0). Setting it restores the default CTA
+ * count for the shape (one wave); fv_get_launch then reports the shape's
+ * resident CTAs. No reference counterpart. */
+fv_status fv_set_cta_shape(fv_handle *h, int32_t shape);
+fv_status fv_get_cta_shape(fv_handle *h, int32_t *shape, int32_t *warps_per_cta);
+
 /* Division in the step kernel, for the autotuner. Both give the same
  * results bit for bit (IEEE-equal quotients everywhere):
  *   FV_DIVISION_FMA: FMA-based division, with a fix-up pass that recomputes

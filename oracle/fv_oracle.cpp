@@ -166,11 +166,11 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
         } else if (i <= 1) {
           if (app == FV_APP_HIFU_BEAM) {
             // hifu :77-107
-            int width = static_cast<int>(ac.ispa / dy);
+            int width = static_cast<int>(double(ac.ispa / dy));
             int jprime = j - 2;
             if (std::abs(jprime) < width && jprime >= 0 && mdx == 0) {
               R jprime2 = static_cast<R>(jprime * jprime);
-              R nudenom = std::sqrt(jprime2 + ac.ispf * ac.ispf);
+              R nudenom = osqrt(jprime2 + ac.ispf * ac.ispf);
               R nux = ac.ispf / nudenom;
               R nuy = -static_cast<R>(jprime) / nudenom;
               R phi = (dx * jprime2) / (R(2) * ac.ispf);
@@ -197,9 +197,9 @@ void Sim<R>::boundary(std::vector<R> const *in, std::vector<R> *out) {
             }
           } else if (app == FV_APP_FOCUSED_BEAM) {
             R jp = R(j) - ac.center;
-            if (std::fabs(jp) < ac.aperture && mdx == 0) {
+            if (ofabs(jp) < ac.aperture && mdx == 0) {
               R jp2 = jp * jp;
-              R nudenom = std::sqrt(jp2 + ac.ispf * ac.ispf);
+              R nudenom = osqrt(jp2 + ac.ispf * ac.ispf);
               R nux = ac.ispf / nudenom;
               R nuy = -jp / nudenom;
               R phi = (dx * jp2) / (R(2) * ac.ispf);
@@ -359,6 +359,7 @@ template <class R> R Sim<R>::reduce_cfl() const {
 }
 
 template <class R> int Sim<R>::attempt(int stop_stage) {
+  last_dt = dt;
   boundary(u, s0);
   if (stop_stage == FV_STAGE_BOUNDARY) return 0;
   if (!sweep(1, s0, s1a, s1)) { status = FV_NEGATIVE_EIGENVALUE; return 2; }
@@ -378,8 +379,8 @@ template <class R> int Sim<R>::attempt(int stop_stage) {
     n = n + 1;
     if (p.moving_domain && T >= ac.mdt) {
       // moveDomain + updateMDXY, common/main.cu:109-177
-      const int mdi = static_cast<int>((T - ac.mdt) * R(p.mdvx) / dx) - mdx;
-      const int mdj = static_cast<int>((T - ac.mdt) * R(p.mdvy) / dy) - mdy;
+      const int mdi = static_cast<int>(double((T - ac.mdt) * R(p.mdvx) / dx)) - mdx;
+      const int mdj = static_cast<int>(double((T - ac.mdt) * R(p.mdvy) / dy)) - mdy;
       for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) {
           int ir = i + mdi, jr = j + mdj;
@@ -426,6 +427,72 @@ template <class R> int Sim<R>::run(int64_t nsteps) {
 
 template class Sim<float>;
 template class Sim<double>;
+
+// The tangent-linear model: the same step on dual numbers (fv_dual.hpp),
+// with up to kTlmDirs derivative directions.
+constexpr int kTlmDirs = 16;
+template class Sim<Dual<float, kTlmDirs>>;
+template class Sim<Dual<double, kTlmDirs>>;
+
+// The working type of tlm_loss: duals with K directions, or the plain type
+// for K = 0 (the loss alone).
+template <class V, int K> struct TlmType { using type = Dual<V, K>; };
+template <class V> struct TlmType<V, 0> { using type = V; };
+template <class V, int K> static inline void seed(Dual<V, K> &x, int r) { x.d[r] = 1.0; }
+template <class V> static inline void seed(V &, int) {}
+template <class V, int K> static inline double deriv(const Dual<V, K> &x, int r) { return x.d[r]; }
+template <class V> static inline double deriv(const V &, int) { return 0.0; }
+template <class V, int K> static inline double value(const Dual<V, K> &x) { return double(x.v); }
+template <class V> static inline double value(const V &x) { return double(x); }
+
+// Loss and its derivatives along the seeded directions: the phased array's
+// weights (amplitudes [0, nelem), phases [nelem, 2 nelem)) are the inputs;
+// the dt schedule is held fixed (dts[n], Ts[n]: dt and T of accepted step
+// n), as the library's adjoint holds it; loss = mean of u1^2 over the
+// window [i0, i0+ni) x [j0, j0+nj) and accepted steps first..last.
+template <class V, int K = kTlmDirs>
+static int tlm_loss(const fv_params *p, bool fvm, const double *amp, const double *phase, int nelem, int ndir,
+                    const int *dir_param, int64_t nsteps, const double *dts, const double *Ts, const int *win,
+                    double *loss, double *grad) {
+  using D = typename TlmType<V, K>::type;
+  if (ndir < 0 || ndir > K || p->app != FV_APP_PHASED_ARRAY || nelem != p->array_elems) return FV_BAD_ARG;
+  fv_params q = *p;
+  q.cflmax = 1e30;  // the schedule is given: every attempt is accepted
+  Sim<D> s(q, fvm);
+  for (int k = 0; k < nelem; ++k) {
+    s.ac.amp[k] = D(amp[k]);
+    s.ac.phase[k] = D(phase[k]);
+  }
+  for (int r = 0; r < ndir; ++r) {
+    const int idx = dir_param[r];
+    if (idx < 0 || idx >= 2 * nelem) return FV_BAD_ARG;
+    if (idx < nelem) seed(s.ac.amp[idx], r);
+    else seed(s.ac.phase[idx - nelem], r);
+  }
+  s.init_state();
+  const int i0 = win[0], j0 = win[1], ni = win[2], nj = win[3], first = win[4], last = win[5];
+  double acc = 0.0, accd[kTlmDirs + 1] = {};
+  for (int64_t n = 0; n < nsteps; ++n) {
+    s.dt = D(dts[n]);
+    s.T = D(Ts[n]);
+    s.n = int32_t(n);
+    const int r = s.attempt();
+    if (r != 0) return r == 2 ? FV_NEGATIVE_EIGENVALUE : FV_DT_TOO_LARGE;
+    if (n + 1 >= first && n + 1 <= last) {
+      for (int j = j0; j < j0 + nj; ++j)
+        for (int i = i0; i < i0 + ni; ++i) {
+          const D &u1 = s.u[0][s.off(i, j)];
+          const double v = value(u1);
+          acc += v * v;
+          for (int k = 0; k < ndir; ++k) accd[k] += 2.0 * v * deriv(u1, k);
+        }
+    }
+  }
+  const double cnt = double(last - first + 1) * double(ni) * double(nj);
+  *loss = acc / cnt;
+  for (int k = 0; k < ndir; ++k) grad[k] = accd[k] / cnt;
+  return FV_OK;
+}
 
 }  // namespace fvo
 
@@ -599,6 +666,44 @@ void fvo_fvm_eval(int fn, const float *x, float *y, int64_t n) {
       default: y[k] = fvm::tanhf_(x[k]); break;
     }
   }
+}
+
+// The loss alone on a fixed schedule (tlm_loss's loss without derivatives),
+// in FP32 (prec 4) or FP64 (prec 8): the central differences' evaluations.
+int fvo_schedule_loss(const fv_params *p, int prec, int flags, const double *amp, const double *phase, int nelem,
+                      int64_t nsteps, const double *dts, const double *Ts, const int *win, double *loss) {
+  if (!p || !amp || !phase || !dts || !Ts || !win || !loss) return FV_BAD_ARG;
+  const bool m = (flags & 1) != 0;
+  const int dummy = 0;
+  double g = 0.0;
+  if (prec == 4)
+    return fvo::tlm_loss<float, 0>(p, m, amp, phase, nelem, 0, &dummy, nsteps, dts, Ts, win, loss, &g);
+  if (prec == 8)
+    return fvo::tlm_loss<double, 0>(p, m, amp, phase, nelem, 0, &dummy, nsteps, dts, Ts, win, loss, &g);
+  return FV_BAD_ARG;
+}
+
+// The tangent-linear gradient (tlm_loss above) in FP32 values (prec 4:
+// along the FP32 oracle's trajectory, which the CUDA path reproduces bit for
+// bit) or FP64 values (prec 8); derivatives are double either way. win:
+// i0, j0, ni, nj, first, last.
+int fvo_tlm_loss(const fv_params *p, int prec, int flags, const double *amp, const double *phase, int nelem,
+                 int ndir, const int *dir_param, int64_t nsteps, const double *dts, const double *Ts,
+                 const int *win, double *loss, double *grad) {
+  if (!p || !amp || !phase || !dir_param || !dts || !Ts || !win || !loss || !grad) return FV_BAD_ARG;
+  const bool m = (flags & 1) != 0;
+  if (prec == 4)
+    return fvo::tlm_loss<float>(p, m, amp, phase, nelem, ndir, dir_param, nsteps, dts, Ts, win, loss, grad);
+  if (prec == 8)
+    return fvo::tlm_loss<double>(p, m, amp, phase, nelem, ndir, dir_param, nsteps, dts, Ts, win, loss, grad);
+  return FV_BAD_ARG;
+}
+
+// dt of the attempt that fvo_run accepted last (the schedule of a run).
+double fvo_last_dt(void *hv) {
+  Handle *h = static_cast<Handle *>(hv);
+  if (!h) return -1.0;
+  return h->prec == 4 ? double(h->f->last_dt) : h->d->last_dt;
 }
 
 // The CFL of the step that fvo_debug_step or fvo_run attempted last.

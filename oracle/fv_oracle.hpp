@@ -31,6 +31,7 @@
 
 #include "../include/fivonagi.h"
 #include "../fivonagi_gb300/csrc/fv_math.h"
+#include "fv_dual.hpp"
 
 namespace fvo {
 
@@ -54,6 +55,28 @@ template <> struct Fn<double> {
   static double tanh(double x, bool m) { return m ? fvm::tanh_d(x) : std::tanh(x); }
 };
 
+// The tangent-linear model's dual numbers: values as the plain type's,
+// derivatives by the chain rule (fv_dual.hpp).
+template <class V, int K> struct Fn<Dual<V, K>> {
+  using D = Dual<V, K>;
+  static D sin(const D &x, bool m) { return dchain(Fn<V>::sin(x.v, m), std::cos(double(x.v)), x); }
+  static D cos(const D &x, bool m) { return dchain(Fn<V>::cos(x.v, m), -std::sin(double(x.v)), x); }
+  static D exp(const D &x, bool m) {
+    const V e = Fn<V>::exp(x.v, m);
+    return dchain(e, std::exp(double(x.v)), x);
+  }
+  static D tanh(const D &x, bool m) {
+    const double t = std::tanh(double(x.v));
+    return dchain(Fn<V>::tanh(x.v, m), 1.0 - t * t, x);
+  }
+};
+
+// sqrt and fabs of the working type (the plain types' own, or the duals')
+template <class R> static inline R osqrt(R x) { return std::sqrt(x); }
+template <class R> static inline R ofabs(R x) { return std::fabs(x); }
+template <class V, int K> static inline Dual<V, K> osqrt(Dual<V, K> x) { return dsqrt(x); }
+template <class V, int K> static inline Dual<V, K> ofabs(Dual<V, K> x) { return dfabs(x); }
+
 // getmax / getmin exactly as common/main.cu:63-69: the second argument wins
 // ties and NaN comparisons.
 template <class R> static inline R getmax(R x, R y) { return (x > y) ? x : y; }
@@ -65,6 +88,9 @@ template <> struct Consts<float> {
 };
 template <> struct Consts<double> {
   static double pi() { return 3.141592653589793; }  // common/numbers.h:15-16
+};
+template <class V, int K> struct Consts<Dual<V, K>> {
+  static Dual<V, K> pi() { return Dual<V, K>::of(Consts<V>::pi()); }
 };
 
 // The Riemann solution at one interface, in the sweep's local frame:
@@ -92,8 +118,8 @@ static inline bool riemann(R rho_a, R un_a, R ut_a, R rho_b, R un_b, R ut_b,
   R tmp2 = (Zn * Zn) / Z1;
   R tmp3 = tmp1 * tmp1 - n2 * tmp2 + n1 + n2 * (beta - n1) * (Z1 - n1);
   if (tmp3 < n0) return false;
-  R L1 = tmp1 + std::sqrt(tmp3);
-  R L2 = tmp1 - std::sqrt(tmp3);
+  R L1 = tmp1 + osqrt(tmp3);
+  R L2 = tmp1 - osqrt(tmp3);
   R L3 = tmp1;
   R A1 = (L1 * Zt - n2 * Zn * Zt) / (L1 * Z1 - Zt);
   R A2 = (L2 * Zt - n2 * Zn * Zt) / (L2 * Z1 - Zt);
@@ -171,7 +197,7 @@ static inline void correction(const Wave<R> &wm, const Wave<R> &w0,
   dotr = z * z + z * z + w0.w33 * wp.w33;
   dotl = z * z + z * z + w0.w33 * wm.w33;
   R l3 = mc_limit(wnorm2, dotl, dotr, w0.s3);
-  R a1 = std::fabs(w0.s1), a2 = std::fabs(w0.s2), a3 = std::fabs(w0.s3);
+  R a1 = ofabs(w0.s1), a2 = ofabs(w0.s2), a3 = ofabs(w0.s3);
   R c1 = a1 * (n1 - a1 * dtx) * w0.w11 * l1 + a2 * (n1 - a2 * dtx) * w0.w12 * l2 +
          a3 * (n1 - a3 * dtx) * z * l3;
   R c2 = a1 * (n1 - a1 * dtx) * w0.w21 * l1 + a2 * (n1 - a2 * dtx) * w0.w22 * l2 +
@@ -208,6 +234,7 @@ template <class R> class Sim {
   int32_t n = 0, mdx = 0, mdy = 0;
   int status = 0;
   R last_cfl{};
+  R last_dt{};  // dt of the last attempt
   int64_t accepted = 0, rejected = 0;
   int rejected_last = 0;  // the reference's device simError == 1 after a rejection
   // state (the A/B pair holds the same values between steps)

@@ -67,6 +67,14 @@ def _load_oracle() -> C.CDLL:
         lib.fvo_fvm_eval.argtypes = [C.c_int, P, P, C.c_int64]
         lib.fvo_set_weights.restype = C.c_int
         lib.fvo_set_weights.argtypes = [P, P, P, C.c_int]
+        lib.fvo_last_dt.restype = C.c_double
+        lib.fvo_last_dt.argtypes = [P]
+        lib.fvo_schedule_loss.restype = C.c_int
+        lib.fvo_schedule_loss.argtypes = [C.POINTER(FvParams), C.c_int, C.c_int, P, P, C.c_int, C.c_int64, P, P,
+                                          P, P]
+        lib.fvo_tlm_loss.restype = C.c_int
+        lib.fvo_tlm_loss.argtypes = [C.POINTER(FvParams), C.c_int, C.c_int, P, P, C.c_int, C.c_int, P,
+                                     C.c_int64, P, P, P, P, P]
         _oracle = lib
     return _oracle
 
@@ -175,6 +183,49 @@ class OracleSim:
     def last_cfl(self) -> float:
         return self.lib.fvo_last_cfl(self.h)
 
+    def last_dt(self) -> float:
+        """dt of the attempt that the last run(1) accepted."""
+        return self.lib.fvo_last_dt(self.h)
+
+    def schedule(self, nsteps: int):
+        """Run nsteps accepted steps one at a time; returns (dts, Ts): dt and
+        T (before the step) of each accepted step, the schedule the
+        library's adjoint holds fixed."""
+        dts = np.empty(nsteps, np.float64)
+        Ts = np.empty(nsteps, np.float64)
+        for n in range(nsteps):
+            Ts[n] = self.stats()["T"]
+            st = self.run(1)
+            if st["rc"] != 0:
+                raise RuntimeError(f"oracle stopped with status {st['rc']} at step {n}")
+            dts[n] = self.last_dt()
+        return dts, Ts
+
+
+def tlm_loss(params: FvParams, amp, phase, directions, dts, Ts, window, dtype=np.float64, math="fvm"):
+    """The oracle's tangent-linear model of the phased array's windowed loss
+    on a fixed dt schedule: (loss, d loss / d theta_r for each direction r).
+    `directions` index the weights: k < nelem is amp[k], else phase[k -
+    nelem] (at most 16). window = (i0, j0, ni, nj, first, last). dtype
+    float32 runs the values along the FP32 oracle's trajectory, float64
+    along the FP64 one; derivatives are double either way."""
+    lib = _load_oracle()
+    a = np.ascontiguousarray(amp, np.float64)
+    ph = np.ascontiguousarray(phase, np.float64)
+    d = np.ascontiguousarray(directions, np.int32)
+    dts = np.ascontiguousarray(dts, np.float64)
+    Ts = np.ascontiguousarray(Ts, np.float64)
+    w = np.ascontiguousarray(window, np.int32)
+    loss = np.zeros(1, np.float64)
+    grad = np.zeros(len(d), np.float64)
+    p = params.copy()
+    rc = lib.fvo_tlm_loss(C.byref(p), np.dtype(dtype).itemsize, 1 if math == "fvm" else 0, _ptr(a), _ptr(ph),
+                          int(a.size), int(d.size), _ptr(d), int(dts.size), _ptr(dts), _ptr(Ts), _ptr(w),
+                          _ptr(loss), _ptr(grad))
+    if rc != 0:
+        raise RuntimeError(f"fvo_tlm_loss failed with status {rc}")
+    return float(loss[0]), grad
+
 
 def ref_call(params: FvParams, op: int, u, dtype=np.float32, nsteps: int = 0, scalars=None):
     """Call the reference shim: op 0 init, 1 run nsteps, 10+stage debug step.
@@ -195,3 +246,21 @@ def ref_call(params: FvParams, op: int, u, dtype=np.float32, nsteps: int = 0, sc
     p = params.copy()
     rc = fn(C.byref(p), int(op), int(nsteps), *[_ptr(a) for a in u], _ptr(scalars), C.byref(st))
     return rc, st.as_dict()
+
+
+def schedule_loss(params: FvParams, amp, phase, dts, Ts, window, dtype=np.float64, math="fvm") -> float:
+    """The phased array's windowed loss on a fixed dt schedule (tlm_loss's
+    loss without derivatives): the evaluations of central differences."""
+    lib = _load_oracle()
+    a = np.ascontiguousarray(amp, np.float64)
+    ph = np.ascontiguousarray(phase, np.float64)
+    dts = np.ascontiguousarray(dts, np.float64)
+    Ts = np.ascontiguousarray(Ts, np.float64)
+    w = np.ascontiguousarray(window, np.int32)
+    loss = np.zeros(1, np.float64)
+    p = params.copy()
+    rc = lib.fvo_schedule_loss(C.byref(p), np.dtype(dtype).itemsize, 1 if math == "fvm" else 0, _ptr(a), _ptr(ph),
+                               int(a.size), int(dts.size), _ptr(dts), _ptr(Ts), _ptr(w), _ptr(loss))
+    if rc != 0:
+        raise RuntimeError(f"fvo_schedule_loss failed with status {rc}")
+    return float(loss[0])

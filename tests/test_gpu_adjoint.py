@@ -92,6 +92,42 @@ def test_adjoint_gradient_matches_fp64_central_differences():
         assert abs(got - fd) <= 2e-3 * scale, (which, k, got, fd)
 
 
+def test_adjoint_gradient_matches_the_tangent_linear_model_per_component():
+    """Every one of the 16 weights against the oracle's tangent-linear model
+    along the same FP32 trajectory (the dual-number restatement), each
+    within 1e-3 of its own value, and the FP64 tangent-linear model against
+    FP64 central differences."""
+    from oracle.oracle import schedule_loss, tlm_loss
+
+    p = _params()
+    amp, ph = array_weights(p.array_elems, 11, p.ampl)
+    adj = Adjoint(p, loss_window(*WIN), NSTEPS, checkpoint_every=16)
+    loss = adj.forward(amp, ph)
+    ga, gp = adj.backward()
+    dts, Ts = adj.schedule()
+    adj.close()
+    nelem = p.array_elems
+    dirs = list(range(2 * nelem))
+    l32, t32 = tlm_loss(p, amp, ph, dirs, dts, Ts, WIN, np.float32)
+    assert abs(l32 - loss) <= 1e-9 * loss
+    g = np.concatenate([ga, gp])
+    rel = np.abs(g - t32) / np.abs(t32)
+    print("small adjoint vs TLM32, per weight:", np.array2string(rel, precision=2))
+    assert np.all(rel <= 1e-3), rel
+    _, t64 = tlm_loss(p, amp, ph, dirs[:4] + dirs[nelem:nelem + 4], dts, Ts, WIN, np.float64)
+    for r, k in enumerate(dirs[:4] + dirs[nelem:nelem + 4]):
+        a = amp.astype(np.float64).copy()
+        f = ph.astype(np.float64).copy()
+        v, kk = (a, k) if k < nelem else (f, k - nelem)
+        h = 1e-4 * (abs(v[kk]) if k < nelem else max(abs(v[kk]), 1.0))
+        v[kk] += h
+        lp = schedule_loss(p, a, f, dts, Ts, WIN)
+        v[kk] -= 2 * h
+        lm = schedule_loss(p, a, f, dts, Ts, WIN)
+        fd = (lp - lm) / (2 * h)
+        assert abs(t64[r] - fd) <= 1e-3 * abs(fd), (k, t64[r], fd)
+
+
 def test_torch_function_returns_the_adjoint_gradients():
     torch = pytest.importorskip("torch")
     p = _params()
@@ -139,3 +175,4 @@ def test_backward_repeats_and_keeps_the_final_state():
         assert same_values(before[f], after[f])
     assert np.array_equal(ga1, ga2) and np.array_equal(gp1, gp2)
     adj.close()
+

@@ -3,7 +3,7 @@
 The step kernel divides with Markstein's FMA sequence (fvgb::DivFma in
 fv_device.cuh) and leaves the rows where an operand falls outside the range
 in which that sequence is proven to round correctly to a recomputation with
-exact division (fvgb::DivExact). This test builds tests/probes/division_probe.cu against
+exact division (fvgb::DivExact). This test builds tests/native/division_probe.cu against
 the same header and runs it: an exhaustive check of the reciprocal for
 every divisor in range, and sampled quotients around every bound of the
 safety check; every quotient the check lets through must equal the IEEE
@@ -31,7 +31,7 @@ def test_fma_division_is_ieee_where_not_flagged(tmp_path):
     exe = str(tmp_path / "division_probe")
     subprocess.run([_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
                     "-I", os.path.join(ROOT, "fivonagi_gb300", "csrc"), "-o", exe,
-                    os.path.join(ROOT, "tests", "probes", "division_probe.cu")], check=True)
+                    os.path.join(ROOT, "tests", "native", "division_probe.cu")], check=True)
     out = subprocess.run([exe, "200000000"], capture_output=True, text=True, timeout=600)
     rows = {}
     for line in out.stdout.splitlines():

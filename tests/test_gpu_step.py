@@ -433,3 +433,30 @@ def test_few_ctas_match_oracle(app, nx, ny, blocks):
     for f in range(3):
         assert same_values(g[f], o[f]), f"field {f}: rel L2 {rel_l2(g[f], o[f]):.3e}"
     sim.close()
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3])
+@pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (1, 64, 64), (0, 100, 37)])
+def test_cta_shapes_match_oracle(shape, app, nx, ny):
+    """Every CTA shape of the step kernel (warps per CTA x CTAs per SM),
+    at its default CTA count and at a few CTAs, gives the oracle's result."""
+    p = small_params(app, nx, ny)
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    u = perturbed(orc.get_state(), 21, 1e-4)
+    orc.set_state(*u)
+    so = orc.run(30)
+    o = orc.get_state()
+    for blocks in (0, 3):
+        sim = Simulation(p)
+        sim.set_cta_shape(shape)
+        assert sim.get_cta_shape()[0] == shape
+        if blocks:
+            sim.set_launch(blocks)
+        sim.set_state(*u)
+        sg = sim.run(30)
+        assert sg["rejected"] == so["rejected"]
+        g = sim.get_state()
+        for f in range(3):
+            assert same_values(g[f], o[f]), f"shape {shape} blocks {blocks} field {f}"
+        sim.close()

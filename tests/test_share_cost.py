@@ -18,7 +18,7 @@ def test_share_cost_tiles_every_window_row_once(tmp_path):
         pytest.skip("g++ not found")
     exe = str(tmp_path / "share_cost_check")
     subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "fivonagi_gb300", "csrc"), "-o", exe,
-                    os.path.join(ROOT, "tests", "probes", "share_cost_check.cpp")], check=True)
+                    os.path.join(ROOT, "tests", "native", "share_cost_check.cpp")], check=True)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.strip().startswith("share_cost ok"), out.stdout
