@@ -805,37 +805,67 @@ def run_adjoint(args):
     return 0
 
 
-def run_designs(args):
-    """Config 5: designs of the phased array on 2048x1024 (6000 steps), each
-    with its own random weights and a focal target from an 8x8 grid in the
-    right half (a seeded permutation).
-
-    The throughput runs `--concurrent` designs at a time from host threads,
-    each on its own adjoint handle and non-blocking stream (the library's
-    calls release the GIL): the kernels of one design fill the gaps that the
-    small per-step launches of another leave. The backward/forward ratio is
-    timed on the first designs run alone."""
+def designs_report(args, batch: int) -> dict:
+    """Config 5: designs of the phased array on 2048x1024 (6000 steps),
+    each with its own random weights and a focal target from an 8x8 grid in
+    the right half (a seeded permutation), `batch` designs per
+    fv_adjoint_batch (every forward attempt, replayed step and reverse step
+    one launch sequence over the batch). Beside it: the plain forward of one
+    design, the gradient cost per design over it, and the designs run one
+    handle per design on `--concurrent` streams (the previous method), whose
+    gradients must equal the batched ones bit for bit."""
     from concurrent.futures import ThreadPoolExecutor
 
     import numpy as np
     import torch
 
-    from fivonagi_gb300 import _abi
-    from fivonagi_gb300.adjoint import Adjoint
+    from fivonagi_gb300 import Simulation, _abi
+    from fivonagi_gb300.adjoint import Adjoint, AdjointBatch
 
     base = _abi.default_params("phased-array")
     p = base.replace(nx=2048, ny=1024, xmax=2047 / 24, ymax=1023 / 24, center=512.0)
     nsteps = args.adjoint_steps or 6000
-    warm = min(200, nsteps)
     rng = np.random.default_rng(args.seed)
     targets = [(1024 + 128 * (k % 8) + 64, 128 * (k // 8) + 64) for k in rng.permutation(64)]
     cases = [_adjoint_case(p, targets[d], nsteps, args.seed + 1000 + d) for d in range(args.designs)]
-    # ---- alone: the backward/forward ratio and a gradient check
-    _time_design(p, *_adjoint_case(p, targets[0], warm, args.seed), warm)  # warm-up
-    alone = [_time_design(p, *cases[d], nsteps, fd_params=1 if d == 0 else 0)
-             for d in range(min(args.designs, args.ratio_designs))]
+    # plain forward of one design (the cost unit)
+    sim = Simulation(p)
+    sim.set_array_weights(cases[0][0], cases[0][1])
+    sim.init_state()
+    sim.run(min(200, nsteps))
+    sim.init_state()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.run(nsteps)
+    t_plain = time.perf_counter() - t0
+    sim.close()
+    # batched: every design, `batch` at a time
+    mem0 = _device_mem_used()
+    t_fwd = t_bwd = 0.0
+    grads = [None] * args.designs
+    peak = 0
+    for b0 in range(0, args.designs, batch):
+        ds = list(range(b0, min(args.designs, b0 + batch)))
+        ab = AdjointBatch(p, [cases[d][2] for d in ds], nsteps)
+        peak = max(peak, _device_mem_used() - mem0)
+        amp = np.stack([cases[d][0] for d in ds])
+        ph = np.stack([cases[d][1] for d in ds])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ab.forward(amp, ph)
+        t1 = time.perf_counter()
+        ga, gp = ab.backward()
+        t2 = time.perf_counter()
+        t_fwd += t1 - t0
+        t_bwd += t2 - t1
+        for k, d in enumerate(ds):
+            grads[d] = (ga[k], gp[k])
+        ab.close()
+    t_batched = t_fwd + t_bwd
+    # the previous method: one handle per design, `concurrent` streams
+    conc = max(1, args.concurrent)
+    n_conc = min(args.designs, args.conc_designs)
 
-    # ---- throughput: every design, `concurrent` at a time
     def gradient(d):
         amp, ph, win = cases[d]
         adj = Adjoint(p, win, nsteps)
@@ -845,37 +875,56 @@ def run_designs(args):
         finally:
             adj.close()
 
-    conc = max(1, args.concurrent)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     with ThreadPoolExecutor(conc) as ex:
-        grads = list(ex.map(gradient, range(args.designs)))
+        conc_grads = list(ex.map(gradient, range(n_conc)))
     torch.cuda.synchronize()
-    t_all = time.perf_counter() - t0
-    # the concurrent runs give the gradients of the runs alone, bit for bit
-    same = all(np.array_equal(grads[d][0], alone[d]["ga"]) and np.array_equal(grads[d][1], alone[d]["gp"])
-               for d in range(len(alone)))
+    t_conc = time.perf_counter() - t0
+    same = all(np.array_equal(conc_grads[d][0], grads[d][0]) and np.array_equal(conc_grads[d][1], grads[d][1])
+               for d in range(n_conc))
+    return {
+        "value": args.designs / t_batched, "unit": "gradients/s",
+        "designs": args.designs, "designs_per_batch": batch, "steps": nsteps,
+        "forward_plain_s": t_plain,
+        "recorded_forward_s_per_design": t_fwd / args.designs,
+        "backward_s_per_design": t_bwd / args.designs,
+        "gradient_over_forward": t_batched / args.designs / t_plain,
+        "adjoint_forward_ratio": t_bwd / args.designs / t_plain,
+        "peak_adjoint_memory_gb": peak / 1e9,
+        "streams": {"value": n_conc / t_conc, "designs": n_conc, "concurrent": conc,
+                    "method": "one fv_adjoint per design, each on its own stream from a host thread"},
+        "batched_gradients_equal_alone": bool(same),
+        "workload": f"phased array 2048x1024, {nsteps} steps, 128 elements x (amplitude, phase), 32x32 focal "
+                    f"windows from an 8x8 grid in the right half, seed {args.seed}",
+    }
+
+
+def run_designs(args):
+    """Config 5 alone (designs_report), as its own JSON line."""
+    import torch
+
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    sampler = ClockSampler(local)
+    sampler.start()
+    r = designs_report(args, args.designs_per_batch)
+    clocks = sampler.stop()
     line = {
         "metric": "gradients/s",
-        "value": args.designs / t_all,
+        "value": r["value"],
         "unit": "gradients/s",
         "n_gpus": 1,
-        "steps": nsteps,
-        "warmup": warm,
+        "steps": r["steps"],
+        "warmup": 0,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.designs} phased-array designs 2048x1024, {nsteps} steps, 256 weights each, "
-                               "32x32 focal windows from an 8x8 grid in the right half", "seed": args.seed,
-                   "concurrent_designs": conc},
-        "gradients_per_s_alone": len(alone) / sum(r["t_fwd"] + r["t_bwd"] for r in alone),
-        "adjoint_forward_ratio_mean": float(np.mean([r["t_bwd"] / r["t_plain"] for r in alone])),
-        "ratio_designs": len(alone),
-        "concurrent_gradients_equal_alone": bool(same),
-        "adjoint_memory_gb_max": max(r["mem"] for r in alone) / 1e9,
-        "gradient_check": alone[0]["checks"],
+        "config": {"workload": r["workload"], "designs": r["designs"], "designs_per_batch": r["designs_per_batch"]},
+        "designs": r,
+        "clocks": clocks,
     }
     print(json.dumps(line))
     return 0
@@ -902,8 +951,10 @@ def main():
     ap.add_argument("--designs", type=int, default=32)
     ap.add_argument("--concurrent", type=int, default=4,
                     help="designs workload: designs run at a time, each on its own stream")
-    ap.add_argument("--ratio-designs", type=int, default=4,
-                    help="designs workload: designs timed alone for the backward/forward ratio")
+    ap.add_argument("--designs-per-batch", type=int, default=16,
+                    help="designs workload: designs per fv_adjoint_batch (about 10 GB each at 2048x1024, 6000 steps)")
+    ap.add_argument("--conc-designs", type=int, default=8,
+                    help="designs workload: designs run one handle per design on streams, for comparison")
     ap.add_argument("--adjoint-steps", type=int, default=0,
                     help="adjoint and designs workloads: steps instead of the configuration's (a small "
                          "case for a profiler's launch list)")

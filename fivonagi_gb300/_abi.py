@@ -206,6 +206,13 @@ PROTOTYPES = {
     "fv_adjoint_replay": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "fv_adjoint_schedule": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fv_adjoint_get_state": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "fv_adjoint_batch_create": (C.c_int, [C.POINTER(FvParams), C.c_int32, C.POINTER(FvLossWindow), C.c_int64,
+                                          C.c_int32, C.POINTER(_P)]),
+    "fv_adjoint_batch_destroy": (C.c_int, [_P]),
+    "fv_adjoint_batch_set_stream": (C.c_int, [_P, _P]),
+    "fv_adjoint_batch_forward": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "fv_adjoint_batch_backward": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "fv_adjoint_batch_schedule": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "fv_filter_u1": (C.c_int, [_P, C.c_double, _P, C.c_int32]),
     "fv_render": (C.c_int, [_P, C.POINTER(FvRenderSpec), _P, C.c_int32]),
     "fv_collect_enable": (C.c_int, [_P, C.POINTER(FvCollectSpec)]),

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <new>
 #include <vector>
 
@@ -121,10 +122,10 @@ __global__ void adj_loss_kernel(const Ctrl *c, G3 s0, G3 s1, int nx, int i0, int
 // instead of a snapshot, a record, a checkpoint and a loss launch; the two
 // slots keep block 0's write of the next snapshot from racing with the
 // other blocks' read of this one.
-__global__ void adj_record_kernel(const Ctrl *c, AdjRec *rec, int parity, float *sched_dt, float *sched_T,
-                                  int nsteps, G3 s0, G3 s1, float *ckpt, size_t stride, size_t ncell, int every,
-                                  int nx, int i0, int j0, int ni, int nj, long long first, long long last,
-                                  double *acc) {
+__device__ __forceinline__ void record_body(const Ctrl *c, AdjRec *rec, int parity, float *sched_dt,
+                                            float *sched_T, int nsteps, const G3 &s0, const G3 &s1, float *ckpt,
+                                            size_t stride, size_t ncell, int every, int nx, int i0, int j0, int ni,
+                                            int nj, long long first, long long last, double *acc) {
   const AdjRec r = rec[parity];
   const int n = c->n;
   const bool accepted = (n == r.n0 + 1) && r.n0 < nsteps;
@@ -167,6 +168,7 @@ __global__ void adj_record_kernel(const Ctrl *c, AdjRec *rec, int parity, float 
     }
   }
 }
+
 
 // Scalars of step n of the frozen schedule (0-based: the step from u_n).
 // With `fix` (the backward's replays, which run without the finalize
@@ -324,7 +326,8 @@ __device__ __forceinline__ Adj3 diffusion_reverse(const DevParams &p, float ddtx
   return Adj3{l0 - fdiv(gvx * vx + gvy * vy, rho), l1 + fdiv(gvx, rho), l2 + fdiv(gvy, rho)};
 }
 
-__global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt, CG3 s, CG3 s2, CG3 lam, G3 li) {
+__device__ __forceinline__ void sweep_x_body(const DevParams &p, float dt, const CG3 &s, const CG3 &s2,
+                                             const CG3 &lam, const G3 &li) {
   const int nx = p.nx, ny = p.ny;
   const int lane = threadIdx.x & 31;
   const long long windows = (nx + kWarpCols - 1) / kWarpCols;
@@ -378,7 +381,8 @@ __global__ void __launch_bounds__(128) adj_sweep_x_kernel(DevParams p, float dt,
 // and the limiter reverses' pending parts in registers. Iteration j loads
 // row j, solves interface j, reverses the limiter at j-1 and the solve at
 // j-2, and writes the input adjoint of row j-3.
-__global__ void __launch_bounds__(128) adj_sweep_y_kernel(DevParams p, float dt, CG3 s, CG3 lo, G3 li, int seg) {
+__device__ __forceinline__ void sweep_y_body(const DevParams &p, float dt, const CG3 &s, const CG3 &lo,
+                                             const G3 &li, int seg) {
   const int nx = p.nx, ny = p.ny;
   const int lane = threadIdx.x & 31;
   const long long strips = (nx + 31) / 32, nseg = (ny + seg - 1) / seg;
@@ -473,7 +477,7 @@ __device__ __forceinline__ bool array_row(const DevParams &p, int j) {
 // (right column pair, top and bottom row pairs, left pair outside the
 // array), zeros (corners) or the source (left pair on the array's rows).
 // The copies' adjoints return to the cells they copy.
-__global__ void adj_boundary_kernel(DevParams p, CG3 lb, G3 lp) {
+__device__ __forceinline__ void boundary_body(const DevParams &p, const CG3 &lb, const G3 &lp) {
   const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
   const int nx = p.nx, ny = p.ny;
   if (i >= nx || j >= ny) return;
@@ -500,11 +504,12 @@ __global__ void adj_boundary_kernel(DevParams p, CG3 lb, G3 lp) {
 // One warp per element: the lanes load the element's ghost cells at once
 // (a strided loop when an element spans more than 16 rows), a warp
 // reduction in FP64 sums them, and lane 0 updates the element's sums.
-__global__ void adj_weights_kernel(DevParams p, float T, CG3 lb, double *g_amp, double *g_ph) {
+__device__ __forceinline__ void weights_body(const DevParams &p, const float *weights, float T, const CG3 &lb,
+                                             double *g_amp, double *g_ph) {
   const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= p.nelem) return;  // warp-uniform
-  const float amp = p.weights[e], ph = p.weights[p.nelem + e];
+  const float amp = weights[e], ph = weights[p.nelem + e];
   const float ramp = gmin(gmax(T * p.ramp, 0.0f), 1.0f);
   const float arg = p.ispw * T + ph;
   const float sn = fvm::sinf_(arg);
@@ -524,13 +529,176 @@ __global__ void adj_weights_kernel(DevParams p, float T, CG3 lb, double *g_amp, 
   }
 }
 
-// Loss gradient of the state after accepted step n: 2 u1 coef on the window.
-__global__ void adj_loss_grad_kernel(const float *u1, float *l1, int nx, int i0, int j0, int ni, int nj,
-                                     float coef) {
+
+}  // namespace
+
+// ========================================================= batched adjoint
+//
+// fv_adjoint_batch: D designs of one grid and one set of physical
+// parameters (each with its own element weights, loss window and adaptive
+// dt schedule) run as one launch sequence: every attempt of the recorded
+// forward is one batched attempt (the batch kernels of fv_step.cu over the
+// D designs) plus one record launch over all designs; every replayed step
+// of the backward is one stage-recording batched attempt; every reverse
+// step is one launch per reverse kernel over all designs (blockIdx.y or
+// blockIdx.z picks the design). The reverse kernels below take their
+// design's buffers from a descriptor array; fv_adjoint launches the same
+// kernels with a one-design array, so the two give the same gradients bit
+// for bit (the reverse kernels are built with FMA contraction, whose
+// choices could differ between two kernels that inline the same body).
+
+namespace {
+
+// Where one design's buffers live (device copy in fv_adjoint_batch::ddesc).
+struct AdjDesign {
+  float *weights;             // amplitudes then phases
+  float *sched_dt, *sched_T;  // nsteps each
+  float *state[2][3];
+  float *ckpt, *seg, *stg;    // bases of nckpt, C + 1 and 3 C states (3 grids each)
+  float *lam[2][3], *tmp[2][3];
+  double *acc;                // loss sum, then gradient sums (2 nelem)
+  Ctrl *ctrl;
+  AdjRec *rec;                // two slots, by attempt parity
+  int i0, j0, ni, nj;
+  long long first, last;
+};
+
+__device__ __forceinline__ CG3 cstate(const float *base, size_t stride, long long k) {
+  return CG3{{base + (size_t(k) * 3 + 0) * stride, base + (size_t(k) * 3 + 1) * stride,
+              base + (size_t(k) * 3 + 2) * stride}};
+}
+// stage grid triple st (0 = B, 1 = S1, 2 = S2) of the segment's k-th step
+__device__ __forceinline__ CG3 cstage(const float *stg, size_t stride, long long k, int st) {
+  return cstate(stg, stride, k * 3 + st);
+}
+__device__ __forceinline__ CG3 cg(const float *const f[3]) { return CG3{{f[0], f[1], f[2]}}; }
+__device__ __forceinline__ G3 gg(float *const f[3]) { return G3{{f[0], f[1], f[2]}}; }
+
+// Every design back to rest: control block (dt = DTINI, T = -TIDE,
+// `remaining` steps), the record slot before attempt 0, the loss sum.
+__global__ void adjb_reset_kernel(const AdjDesign *D, int nd, float dt, float T, long long remaining) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd) return;
+  Ctrl *c = D[d].ctrl;
+  c->dt = dt;
+  c->T = T;
+  c->last_cfl = 0.0f;
+  c->t_stop = __int_as_float(0x7f800000);
+  c->n = 0;
+  c->cur = 0;
+  c->status = 0;
+  c->neg_flag = 0;
+  c->sim_error = 0;
+  c->consecutive_rejects = 0;
+  c->mdx = 0;
+  c->mdy = 0;
+  c->remaining = remaining;
+  c->accepted = 0;
+  c->rejected = 0;
+  c->blocks_done = 0;
+  c->last_accepted = 0;
+  AdjRec &r = D[d].rec[0];
+  r.dt0 = dt;
+  r.T0 = T;
+  r.n0 = 0;
+  r.accepted = 0;
+  D[d].acc[0] = 0.0;
+}
+
+// The record launch of a batched forward attempt (record_body per design).
+__global__ void adjb_record_kernel(const AdjDesign *D, int parity, int nsteps, size_t stride, size_t ncell,
+                                   int every, int nx) {
+  const AdjDesign &a = D[blockIdx.y];
+  record_body(a.ctrl, a.rec, parity, a.sched_dt, a.sched_T, nsteps, gg(a.state[0]), gg(a.state[1]), a.ckpt, stride,
+              ncell, every, nx, a.i0, a.j0, a.ni, a.nj, a.first, a.last, a.acc);
+}
+
+// Before the replay of step n (0-based: the step from u_n, segment slot
+// `slot`): every design's control block from its frozen schedule, its
+// instance's input, output and stage grids in the segment buffers, a
+// negative eigenvalue met by the previous replay counted in `rejected`,
+// and the batch's fix-up header and CFL accumulator reset.
+__global__ void adjb_sched_kernel(const AdjDesign *D, BatchInst *inst, int nd, int n, int slot, size_t stride,
+                                  uint32_t *fix, int32_t *neg, uint32_t *cfl_bits) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d == 0) {
+    fix[0] = 0u;
+    fix[1] = 0u;
+  }
+  if (d >= nd) return;
+  const AdjDesign &a = D[d];
+  Ctrl *c = a.ctrl;
+  if (neg[d]) c->rejected += 1;
+  neg[d] = 0;
+  cfl_bits[d] = 0u;
+  c->dt = a.sched_dt[n];
+  c->T = a.sched_T[n];
+  c->n = n;
+  c->cur = 0;
+  c->status = 0;
+  c->neg_flag = 0;
+  c->sim_error = 0;
+  c->consecutive_rejects = 0;
+  c->mdx = 0;
+  c->mdy = 0;
+  c->remaining = 1;
+  c->t_stop = __int_as_float(0x7f800000);
+  BatchInst &I = inst[d];
+  for (int f = 0; f < 3; ++f) {
+    I.state[0][f] = a.seg + (size_t(slot) * 3 + f) * stride;
+    I.state[1][f] = a.seg + (size_t(slot + 1) * 3 + f) * stride;
+    for (int st = 0; st < 3; ++st) I.stages[3 * st + f] = a.stg + ((size_t(slot) * 3 + st) * 3 + f) * stride;
+  }
+}
+
+// Every design's instance back on its forward state pair.
+__global__ void adjb_forward_inst_kernel(const AdjDesign *D, BatchInst *inst, int nd) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd) return;
+  for (int b = 0; b < 2; ++b)
+    for (int f = 0; f < 3; ++f) inst[d].state[b][f] = D[d].state[b][f];
+}
+
+// Reverse step n (input u_{n-1}, segment slot `slot`): diffusion and x sweep,
+// lam[lc] -> tmp[1].
+__global__ void __launch_bounds__(128) adjb_sweep_x_kernel(DevParams p, const AdjDesign *D, int n, int slot,
+                                                           int lc, size_t stride) {
+  const AdjDesign &a = D[blockIdx.y];
+  sweep_x_body(p, a.sched_dt[n - 1], cstage(a.stg, stride, slot, 1), cstage(a.stg, stride, slot, 2), cg(a.lam[lc]),
+               gg(a.tmp[1]));
+}
+
+// y sweep: tmp[1] -> tmp[0].
+__global__ void __launch_bounds__(128) adjb_sweep_y_kernel(DevParams p, const AdjDesign *D, int n, int slot,
+                                                           int seg, size_t stride) {
+  const AdjDesign &a = D[blockIdx.y];
+  sweep_y_body(p, a.sched_dt[n - 1], cstage(a.stg, stride, slot, 0), cg(a.tmp[1]), gg(a.tmp[0]), seg);
+}
+
+__global__ void adjb_weights_kernel(DevParams p, const AdjDesign *D, int n) {
+  const AdjDesign &a = D[blockIdx.y];
+  weights_body(p, a.weights, a.sched_T[n - 1], cg(a.tmp[0]), a.acc + 1, a.acc + 1 + p.nelem);
+}
+
+// boundary: tmp[0] -> lam[lc ^ 1]
+__global__ void adjb_boundary_kernel(DevParams p, const AdjDesign *D, int lc) {
+  const AdjDesign &a = D[blockIdx.z];
+  boundary_body(p, cg(a.tmp[0]), gg(a.lam[lc ^ 1]));
+}
+
+// The loss gradient of the state after accepted step m (segment slot
+// `slot`, or the final forward state when slot < 0) into lam[lc], for the
+// designs whose loss steps include m.
+__global__ void adjb_loss_grad_kernel(const AdjDesign *D, int m, int slot, int lc, int final_cur, int nx,
+                                      size_t stride) {
+  const AdjDesign &a = D[blockIdx.y];
+  if (m < a.first || m > a.last) return;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ni * nj) return;
-  const size_t o = size_t(i0 + k % ni) + size_t(j0 + k / ni) * nx;
-  l1[o] += 2.0f * u1[o] * coef;
+  if (k >= a.ni * a.nj) return;
+  const float coef = float(1.0 / (double(a.last - a.first + 1) * double(a.ni) * double(a.nj)));
+  const float *u1 = slot < 0 ? a.state[final_cur][0] : a.seg + size_t(slot) * 3 * stride;
+  const size_t o = size_t(a.i0 + k % a.ni) + size_t(a.j0 + k / a.ni) * nx;
+  a.lam[lc][0][o] += 2.0f * u1[o] * coef;
 }
 
 }  // namespace
@@ -572,6 +740,7 @@ struct fv_adjoint {
   int final_cur = 0;           // state[final_cur] holds the last forward's final state
                                // (the backward's replays reuse the control block)
   int exact = 1;
+  AdjDesign *desc = nullptr;   // this design's buffers for the reverse kernels (device, one entry)
 };
 
 namespace {
@@ -640,10 +809,8 @@ fv_status run_forward(fv_adjoint *a, bool record, double *loss) {
       for (long long k = 0; k < todo; ++k, ++attempt) {
         int rc = launch(a, s, -1);
         if (rc != 0) return afail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
-        adj_record_kernel<<<cgrid, 256, 0, a->stream>>>(a->ctrl, a->rec, int(attempt & 1), a->sched,
-                                                         a->sched + a->nsteps, int(a->nsteps), s0, s1, a->ckpt,
-                                                         a->stride, a->ncell, a->every, P.nx, w.i0, w.j0, w.ni,
-                                                         w.nj, w.step_first, w.step_last, a->acc);
+        adjb_record_kernel<<<dim3(cgrid, 1), 256, 0, a->stream>>>(a->desc, int(attempt & 1), int(a->nsteps),
+                                                                  a->stride, a->ncell, a->every, P.nx);
       }
       FVA_CUDA(cudaGetLastError());
       Ctrl c;
@@ -768,8 +935,8 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   // reverse sweeps: grid-stride warps, as many CTAs as are resident at once
   {
     int ox = 0, oy = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ox, adj_sweep_x_kernel, 128, 0) != cudaSuccess || ox < 1) ox = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oy, adj_sweep_y_kernel, 128, 0) != cudaSuccess || oy < 1) oy = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ox, adjb_sweep_x_kernel, 128, 0) != cudaSuccess || ox < 1) ox = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oy, adjb_sweep_y_kernel, 128, 0) != cudaSuccess || oy < 1) oy = 1;
     const long long xwarps = (long long)((p->nx + kWarpCols - 1) / kWarpCols) * p->ny;
     a->sweep_x_blocks = int(std::max(1LL, std::min((long long)ox * a->sms, (xwarps + 3) / 4)));
     // y sweep: enough row segments to fill the resident warps, at least 16 rows each
@@ -797,6 +964,34 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
   for (int k = 0; k < p->array_elems; ++k) w0[k] = float(p->ampl);
   e = cudaMemcpy(a->weights, w0.data(), w0.size() * sizeof(float), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "weights: %s", cudaGetErrorString(e)));
+  {
+    // this design's buffers, as the reverse kernels read them
+    AdjDesign d{};
+    d.weights = a->weights;
+    d.sched_dt = a->sched;
+    d.sched_T = a->sched + nsteps;
+    for (int b = 0; b < 2; ++b)
+      for (int f = 0; f < 3; ++f) {
+        d.state[b][f] = a->state[b][f];
+        d.lam[b][f] = a->lam[b][f];
+        d.tmp[b][f] = a->tmp[b][f];
+      }
+    d.ckpt = a->ckpt;
+    d.seg = a->seg;
+    d.stg = a->stg;
+    d.acc = a->acc;
+    d.ctrl = a->ctrl;
+    d.rec = a->rec;
+    d.i0 = w->i0;
+    d.j0 = w->j0;
+    d.ni = w->ni;
+    d.nj = w->nj;
+    d.first = w->step_first;
+    d.last = w->step_last;
+    e = cudaMalloc(&a->desc, sizeof(AdjDesign));
+    if (e == cudaSuccess) e = cudaMemcpy(a->desc, &d, sizeof(AdjDesign), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "adjoint descriptor: %s", cudaGetErrorString(e)));
+  }
   *out = a;
   return FV_OK;
 }
@@ -813,6 +1008,7 @@ fv_status fv_adjoint_destroy(fv_adjoint *a) {
   if (a->fix) cudaFree(a->fix);
   if (a->sched) cudaFree(a->sched);
   if (a->acc) cudaFree(a->acc);
+  if (a->desc) cudaFree(a->desc);
   if (a->own_stream) cudaStreamDestroy(a->own_stream);
   delete a;
   return FV_OK;
@@ -874,7 +1070,6 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   const fv_params &P = a->params;
   const int nx = P.nx, ny = P.ny, nelem = P.array_elems;
   const fv_loss_window &w = a->win;
-  const float coef = float(1.0 / (double(w.step_last - w.step_first + 1) * double(w.ni) * double(w.nj)));
   const dim3 blk(kBX, kBY), grd((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY);
   const int wthreads = w.ni * w.nj, wblocks = (wthreads + 255) / 256;
   double *g_amp = a->acc + 1, *g_ph = a->acc + 1 + nelem;
@@ -887,9 +1082,8 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   // lambda_N: the loss gradient of the final state
   int lc = 0;  // lam[lc] holds lambda_n
   FVA_CUDA(cudaMemsetAsync(a->lam[lc][0], 0, bytes, a->stream));
-  if (a->nsteps >= w.step_first && a->nsteps <= w.step_last)
-    adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(a->state[a->final_cur][0], a->lam[lc][0], nx, w.i0,
-                                                          w.j0, w.ni, w.nj, coef);
+  adjb_loss_grad_kernel<<<dim3(wblocks, 1), 256, 0, a->stream>>>(a->desc, int(a->nsteps), -1, lc, a->final_cur, nx,
+                                                                  a->stride);
   const long long C = a->every;
   for (long long seg0 = ((a->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, a->nsteps);  // steps seg0+1 .. seg1
@@ -911,27 +1105,21 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
       if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
     for (long long n = seg1; n > seg0; --n) {
-      // reverse of step n, whose input is u_{n-1}
-      float *in[3];
-      for (int f = 0; f < 3; ++f) in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
-      const float dt = a->h_dt[n - 1], T = a->h_T[n - 1];
-      // the recorded boundary-applied, y-swept and x-swept states
-      float *stage[3][3];
-      for (int st = 0; st < 3; ++st)
-        for (int f = 0; f < 3; ++f) stage[st][f] = stage_grid(a, n - 1 - seg0, st, f);
-      float *const *lo = a->lam[lc];
-      float *const *li = a->lam[lc ^ 1];
-      // diffusion (on S2) and x sweep (on S1): lam_n -> tmp1 (adjoint of S1)
-      adj_sweep_x_kernel<<<a->sweep_x_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[1]), cg3(stage[2]),
-                                                                   cg3(lo), g3(a->tmp[1]));
+      // reverse of step n, whose input is u_{n-1} (segment slot n-1-seg0;
+      // its recorded boundary-applied, y-swept and x-swept states are the
+      // slot's stage grids)
+      const int slot = int(n - 1 - seg0);
+      // diffusion (on S2) and x sweep (on S1): lam[lc] -> tmp1 (adjoint of S1)
+      adjb_sweep_x_kernel<<<dim3(a->sweep_x_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot, lc,
+                                                                             a->stride);
       // y sweep on B: tmp1 -> tmp0 (adjoint of B)
-      adj_sweep_y_kernel<<<a->sweep_y_blocks, 128, 0, a->stream>>>(a->dp, dt, cg3(stage[0]), cg3(a->tmp[1]),
-                                                                   g3(a->tmp[0]), a->sweep_y_seg);
-      // boundary: weights, then lam_{n-1}
-      adj_weights_kernel<<<(nelem + 3) / 4, 128, 0, a->stream>>>(a->dp, T, cg3(a->tmp[0]), g_amp, g_ph);
-      adj_boundary_kernel<<<grd, blk, 0, a->stream>>>(a->dp, cg3(a->tmp[0]), g3(li));
-      if (n - 1 >= w.step_first && n - 1 <= w.step_last)
-        adj_loss_grad_kernel<<<wblocks, 256, 0, a->stream>>>(in[0], li[0], nx, w.i0, w.j0, w.ni, w.nj, coef);
+      adjb_sweep_y_kernel<<<dim3(a->sweep_y_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot,
+                                                                             a->sweep_y_seg, a->stride);
+      // boundary: weights, then lam[lc ^ 1] = lam_{n-1}
+      adjb_weights_kernel<<<dim3((nelem + 3) / 4, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n));
+      adjb_boundary_kernel<<<dim3(grd.x, grd.y, 1), blk, 0, a->stream>>>(a->dp, a->desc, lc);
+      adjb_loss_grad_kernel<<<dim3(wblocks, 1), 256, 0, a->stream>>>(a->desc, int(n - 1), slot, lc ^ 1, 0, nx,
+                                                                      a->stride);
       lc ^= 1;
     }
     FVA_CUDA(cudaGetLastError());
@@ -945,6 +1133,396 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   }
   FVA_CUDA(cudaMemcpy(grad_amp, g_amp, sizeof(double) * nelem, cudaMemcpyDeviceToHost));
   FVA_CUDA(cudaMemcpy(grad_phase, g_ph, sizeof(double) * nelem, cudaMemcpyDeviceToHost));
+  return FV_OK;
+}
+
+}  // extern "C"
+
+struct fv_adjoint_batch {
+  fv_params params{};
+  DevParams dp{};
+  int nd = 0;                   // designs
+  long long nsteps = 0;
+  int every = 1, nckpt = 0;
+  int sms = 0;
+  size_t ncell = 0, stride = 0;
+  int exact = 1;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  std::vector<fv_loss_window> win;
+  std::vector<float *> mem;     // per design: all grids
+  std::vector<AdjDesign> hdesc;
+  AdjDesign *ddesc = nullptr;
+  float *small = nullptr;       // weights, schedules of every design
+  double *acc = nullptr;        // per design: 1 + 2 nelem
+  Ctrl *ctrl = nullptr;         // per design
+  AdjRec *rec = nullptr;        // per design: 2 slots
+  // the batch kernels' arguments over the D designs
+  std::vector<BatchInst> hinst;
+  BatchInst *inst = nullptr;
+  uint32_t *cfl_bits = nullptr;
+  int32_t *neg = nullptr;
+  uint32_t *fix = nullptr;
+  size_t fix_words = 0;
+  float *frame = nullptr;
+  BatchArgs args{};
+  int sweep_x_blocks = 0, sweep_y_blocks = 0, sweep_y_seg = 0;
+  std::vector<int> final_cur;
+  bool have_forward = false;
+  std::vector<std::vector<float>> h_dt, h_T;
+};
+
+namespace {
+
+int launch_b(const fv_adjoint_batch *b, bool replay) {
+  if (replay) return b->exact ? launch_batch_replay_exact(b->args, b->stream) : launch_batch_replay_fast(b->args, b->stream);
+  return b->exact ? launch_batch_exact(b->args, b->stream) : launch_batch_fast(b->args, b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+fv_status fv_adjoint_batch_create(const fv_params *p, int32_t ndesigns, const fv_loss_window *windows,
+                                  int64_t nsteps, int32_t checkpoint_every, fv_adjoint_batch **out) {
+  if (!p || !windows || !out || ndesigns < 1 || ndesigns > 1024) return afail(FV_BAD_ARG, "bad argument");
+  *out = nullptr;
+  fv_status s = validate_params(p);
+  if (s != FV_OK) return s;
+  if (p->app != FV_APP_PHASED_ARRAY) return afail(FV_BAD_ARG, "the adjoint is for the phased array app");
+  if (p->moving_domain) return afail(FV_BAD_ARG, "the adjoint needs moving_domain = 0");
+  if (nsteps < 1 || nsteps > (1LL << 24)) return afail(FV_BAD_ARG, "nsteps must be 1..2^24");
+  for (int d = 0; d < ndesigns; ++d) {
+    const fv_loss_window &w = windows[d];
+    if (w.ni < 1 || w.nj < 1 || w.i0 < 0 || w.j0 < 0 || w.i0 + w.ni > p->nx || w.j0 + w.nj > p->ny)
+      return afail(FV_BAD_ARG, "loss window %d outside the grid", d);
+    if (w.step_first < 1 || w.step_last < w.step_first || w.step_last > nsteps)
+      return afail(FV_BAD_ARG, "loss steps of window %d must satisfy 1 <= first <= last <= nsteps", d);
+  }
+  int dev = 0;
+  FVA_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  FVA_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3) return afail(FV_NO_DEVICE, "device is not sm_103");
+  fv_adjoint_batch *b = new (std::nothrow) fv_adjoint_batch();
+  if (!b) return afail(FV_CUDA_ERROR, "out of host memory");
+  auto cleanup = [&](fv_status st) {
+    fv_adjoint_batch_destroy(b);
+    return st;
+  };
+  b->params = *p;
+  b->nd = ndesigns;
+  b->nsteps = nsteps;
+  b->exact = p->exact ? 1 : 0;
+  b->every = checkpoint_every > 0 ? checkpoint_every : std::max(1, int(std::ceil(std::sqrt(double(nsteps)))));
+  b->nckpt = int(nsteps / b->every) + 1;
+  b->ncell = size_t(p->nx) * size_t(p->ny);
+  b->stride = (b->ncell + 63) & ~size_t(63);
+  b->sms = prop.multiProcessorCount;
+  b->dp = dev_params_of(*p);
+  b->win.assign(windows, windows + ndesigns);
+  b->final_cur.assign(ndesigns, 0);
+  b->h_dt.resize(ndesigns);
+  b->h_T.resize(ndesigns);
+  const int nelem = p->array_elems;
+  const size_t nstates = 2 + size_t(b->nckpt) + size_t(b->every + 1) + 3 * size_t(b->every) + 2 + 2;
+  const size_t fcells = size_t(frame_cells(p->nx, p->ny));
+  const size_t fstride = (fcells + 63) & ~size_t(63);
+  cudaError_t e = cudaSuccess;
+  b->mem.assign(ndesigns, nullptr);
+  for (int d = 0; d < ndesigns && e == cudaSuccess; ++d) e = cudaMalloc(&b->mem[d], nstates * 3 * b->stride * sizeof(float));
+  if (e != cudaSuccess)
+    return cleanup(afail(FV_CUDA_ERROR, "cudaMalloc adjoint grids (%d designs of %zu MB): %s", ndesigns,
+                         nstates * 3 * b->stride * 4 >> 20, cudaGetErrorString(e)));
+  const size_t small_per = 2 * size_t(nelem) + 2 * size_t(nsteps);
+  e = cudaMalloc(&b->small, small_per * ndesigns * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&b->acc, (1 + 2 * size_t(nelem)) * ndesigns * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&b->ctrl, sizeof(Ctrl) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->rec, 2 * sizeof(AdjRec) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->ddesc, sizeof(AdjDesign) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->inst, sizeof(BatchInst) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->cfl_bits, sizeof(uint32_t) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->neg, sizeof(int32_t) * ndesigns);
+  if (e == cudaSuccess) e = cudaMalloc(&b->frame, 3 * fstride * ndesigns * sizeof(float));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "adjoint batch allocation: %s", cudaGetErrorString(e)));
+  b->stream = b->own_stream;
+
+  // per design: its grids (as fv_adjoint lays them out), weights, schedule
+  b->hdesc.resize(ndesigns);
+  b->hinst.resize(ndesigns);
+  const int windows_x = (p->nx + kWarpCols - 1) / kWarpCols;
+  long long work = 0, cost = 0, fix_chunks = 0;
+  for (int d = 0; d < ndesigns; ++d) {
+    AdjDesign &a = b->hdesc[d];
+    float *cur = b->mem[d];
+    auto take = [&](size_t nst) {
+      float *r = cur;
+      cur += nst * 3 * b->stride;
+      return r;
+    };
+    for (int k = 0; k < 2; ++k) {
+      float *base = take(1);
+      for (int f = 0; f < 3; ++f) a.state[k][f] = base + f * b->stride;
+    }
+    a.ckpt = take(b->nckpt);
+    a.seg = take(b->every + 1);
+    a.stg = take(3 * size_t(b->every));
+    for (int k = 0; k < 2; ++k) {
+      float *base = take(1);
+      for (int f = 0; f < 3; ++f) a.lam[k][f] = base + f * b->stride;
+    }
+    for (int k = 0; k < 2; ++k) {
+      float *base = take(1);
+      for (int f = 0; f < 3; ++f) a.tmp[k][f] = base + f * b->stride;
+    }
+    float *sm = b->small + small_per * d;
+    a.weights = sm;
+    a.sched_dt = sm + 2 * nelem;
+    a.sched_T = sm + 2 * nelem + nsteps;
+    a.acc = b->acc + (1 + 2 * size_t(nelem)) * d;
+    a.ctrl = b->ctrl + d;
+    a.rec = b->rec + 2 * d;
+    const fv_loss_window &w = windows[d];
+    a.i0 = w.i0;
+    a.j0 = w.j0;
+    a.ni = w.ni;
+    a.nj = w.nj;
+    a.first = w.step_first;
+    a.last = w.step_last;
+
+    BatchInst &I = b->hinst[d];
+    std::memset(&I, 0, sizeof(I));
+    I.p = b->dp;
+    I.p.weights = a.weights;
+    for (int k = 0; k < 2; ++k)
+      for (int f = 0; f < 3; ++f) I.state[k][f] = a.state[k][f];
+    for (int f = 0; f < 3; ++f) I.frame[f] = b->frame + (3 * size_t(d) + f) * fstride;
+    I.ctrl = a.ctrl;
+    I.work_begin = work;
+    I.work = (long long)windows_x * p->ny;
+    work += I.work;
+    I.cost_begin = cost;
+    I.cost = ShareCost(p->nx, p->ny).total();
+    cost += I.cost;
+    I.fix_base = fix_chunks;
+    fix_chunks += (long long)windows_x * fix_chunks_per_window(p->ny);
+  }
+  if (fix_chunks >= (1LL << 32)) return cleanup(afail(FV_BAD_ARG, "batch above 2^32 fix-up chunks"));
+  b->fix_words = size_t(4 + (fix_chunks + 31) / 32 + 2 * fix_chunks);
+  e = cudaMalloc(&b->fix, b->fix_words * sizeof(uint32_t));
+  if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "cudaMalloc fix-up scratch: %s", cudaGetErrorString(e)));
+  FVA_CUDA(cudaMemcpyAsync(b->ddesc, b->hdesc.data(), sizeof(AdjDesign) * ndesigns, cudaMemcpyHostToDevice, b->stream));
+  FVA_CUDA(cudaMemcpyAsync(b->inst, b->hinst.data(), sizeof(BatchInst) * ndesigns, cudaMemcpyHostToDevice, b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->fix, 0, b->fix_words * sizeof(uint32_t), b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->cfl_bits, 0, sizeof(uint32_t) * ndesigns, b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->neg, 0, sizeof(int32_t) * ndesigns, b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->frame, 0, 3 * fstride * ndesigns * sizeof(float), b->stream));
+  {
+    // every design starts with every element at amplitude AMPL and phase 0
+    std::vector<float> w0(2 * size_t(nelem), 0.0f);
+    for (int k = 0; k < nelem; ++k) w0[k] = float(p->ampl);
+    for (int d = 0; d < ndesigns; ++d)
+      FVA_CUDA(cudaMemcpyAsync(b->hdesc[d].weights, w0.data(), w0.size() * sizeof(float), cudaMemcpyHostToDevice,
+                               b->stream));
+    FVA_CUDA(cudaStreamSynchronize(b->stream));  // w0 is a host temporary
+  }
+  const int per_sm = b->exact ? max_batch_blocks_per_sm_exact() : max_batch_blocks_per_sm_fast();
+  const long long resident = (long long)per_sm * b->sms;
+  BatchArgs &A = b->args;
+  A.inst = b->inst;
+  A.cfl_bits = b->cfl_bits;
+  A.neg = b->neg;
+  A.fix = b->fix;
+  A.n = ndesigns;
+  A.work = work;
+  A.cost = cost;
+  A.fix_chunks = fix_chunks;
+  A.max_frame = 4 * p->nx + 4 * (p->ny - 4);
+  A.fix_blocks = 4 * b->sms;
+  // eight waves of resident CTAs (fv_batch's default), at least 128 rows a CTA
+  A.nblocks = int(std::max(1LL, std::min(8 * resident, work / 128)));
+  {
+    int ox = 0, oy = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ox, adjb_sweep_x_kernel, 128, 0) != cudaSuccess || ox < 1) ox = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oy, adjb_sweep_y_kernel, 128, 0) != cudaSuccess || oy < 1) oy = 1;
+    // the y sweep's row segments as for one design; the CTAs of both sweeps
+    // are spread over the designs (gridDim.y)
+    const long long xwarps = (long long)windows_x * p->ny;
+    b->sweep_x_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)ox * b->sms / ndesigns), (xwarps + 3) / 4)));
+    const long long strips = (p->nx + 31) / 32, ywarps = 4LL * oy * b->sms;
+    const long long nseg = std::max(1LL, std::min((long long)(p->ny + 15) / 16, ywarps / strips));
+    b->sweep_y_seg = int((p->ny + nseg - 1) / nseg);
+    const long long ytotal = strips * ((p->ny + b->sweep_y_seg - 1) / b->sweep_y_seg);
+    b->sweep_y_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)oy * b->sms / ndesigns), (ytotal + 3) / 4)));
+  }
+  e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "adjoint batch set-up: %s", cudaGetErrorString(e)));
+  *out = b;
+  return FV_OK;
+}
+
+fv_status fv_adjoint_batch_destroy(fv_adjoint_batch *b) {
+  if (!b) return FV_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (float *m : b->mem)
+    if (m) cudaFree(m);
+  if (b->small) cudaFree(b->small);
+  if (b->acc) cudaFree(b->acc);
+  if (b->ctrl) cudaFree(b->ctrl);
+  if (b->rec) cudaFree(b->rec);
+  if (b->ddesc) cudaFree(b->ddesc);
+  if (b->inst) cudaFree(b->inst);
+  if (b->cfl_bits) cudaFree(b->cfl_bits);
+  if (b->neg) cudaFree(b->neg);
+  if (b->fix) cudaFree(b->fix);
+  if (b->frame) cudaFree(b->frame);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+  return FV_OK;
+}
+
+fv_status fv_adjoint_batch_set_stream(fv_adjoint_batch *b, void *cuda_stream) {
+  if (!b) return afail(FV_BAD_ARG, "NULL argument");
+  FVA_CUDA(cudaStreamSynchronize(b->stream));
+  b->stream = cuda_stream ? (cudaStream_t)cuda_stream : b->own_stream;
+  return FV_OK;
+}
+
+fv_status fv_adjoint_batch_forward(fv_adjoint_batch *b, const float *amp, const float *phase, double *loss) {
+  if (!b || !amp || !phase) return afail(FV_BAD_ARG, "NULL argument");
+  const fv_params &P = b->params;
+  const int nelem = P.array_elems, nd = b->nd;
+  b->have_forward = false;
+  const size_t bytes = 3 * b->stride * sizeof(float);
+  for (int d = 0; d < nd; ++d) {
+    const AdjDesign &a = b->hdesc[d];
+    FVA_CUDA(cudaMemcpyAsync(a.weights, amp + size_t(d) * nelem, sizeof(float) * nelem, cudaMemcpyHostToDevice,
+                             b->stream));
+    FVA_CUDA(cudaMemcpyAsync(a.weights + nelem, phase + size_t(d) * nelem, sizeof(float) * nelem,
+                             cudaMemcpyHostToDevice, b->stream));
+    for (int k = 0; k < 2; ++k) FVA_CUDA(cudaMemsetAsync(a.state[k][0], 0, bytes, b->stream));
+    FVA_CUDA(cudaMemsetAsync(a.ckpt, 0, bytes, b->stream));  // checkpoint 0: the initial state
+  }
+  FVA_CUDA(cudaMemsetAsync(b->fix, 0, b->fix_words * sizeof(uint32_t), b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->cfl_bits, 0, sizeof(uint32_t) * nd, b->stream));
+  FVA_CUDA(cudaMemsetAsync(b->neg, 0, sizeof(int32_t) * nd, b->stream));
+  const int tb = 128, tg = (nd + tb - 1) / tb;
+  adjb_forward_inst_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd);
+  adjb_reset_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, nd, float(P.dtini), -float(P.tide), b->nsteps);
+  FVA_CUDA(cudaGetLastError());
+  const dim3 rgrid(std::max(1, b->sms * 4 / nd), nd);
+  std::vector<Ctrl> hc(nd);
+  long long todo = b->nsteps, attempt = 0;
+  for (int round = 0; round < 64 && todo > 0; ++round) {
+    for (long long k = 0; k < todo; ++k, ++attempt) {
+      const int rc = launch_b(b, false);
+      if (rc != 0) return afail(FV_CUDA_ERROR, "batch step launch: %s", cudaGetErrorString((cudaError_t)rc));
+      adjb_record_kernel<<<rgrid, 256, 0, b->stream>>>(b->ddesc, int(attempt & 1), int(b->nsteps), b->stride,
+                                                        b->ncell, b->every, P.nx);
+    }
+    FVA_CUDA(cudaGetLastError());
+    FVA_CUDA(cudaMemcpyAsync(hc.data(), b->ctrl, sizeof(Ctrl) * nd, cudaMemcpyDeviceToHost, b->stream));
+    FVA_CUDA(cudaStreamSynchronize(b->stream));
+    todo = 0;
+    for (int d = 0; d < nd; ++d) {
+      if (hc[d].status) return afail((fv_status)hc[d].status, "design %d's forward stopped with status %d", d, hc[d].status);
+      todo = std::max<long long>(todo, hc[d].remaining);  // rejected attempts are made up
+    }
+  }
+  if (todo > 0) return afail(FV_DT_TOO_LARGE, "forward run did not finish");
+  for (int d = 0; d < nd; ++d) {
+    const AdjDesign &a = b->hdesc[d];
+    b->final_cur[d] = hc[d].cur & 1;
+    b->h_dt[d].resize(b->nsteps);
+    b->h_T[d].resize(b->nsteps);
+    FVA_CUDA(cudaMemcpy(b->h_dt[d].data(), a.sched_dt, sizeof(float) * b->nsteps, cudaMemcpyDeviceToHost));
+    FVA_CUDA(cudaMemcpy(b->h_T[d].data(), a.sched_T, sizeof(float) * b->nsteps, cudaMemcpyDeviceToHost));
+    double sum = 0.0;
+    FVA_CUDA(cudaMemcpy(&sum, a.acc, sizeof(double), cudaMemcpyDeviceToHost));
+    const fv_loss_window &w = b->win[d];
+    if (loss) loss[d] = sum / (double(w.step_last - w.step_first + 1) * double(w.ni) * double(w.nj));
+  }
+  b->have_forward = true;
+  return FV_OK;
+}
+
+fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, double *grad_phase) {
+  if (!b || !grad_amp || !grad_phase) return afail(FV_BAD_ARG, "NULL argument");
+  if (!b->have_forward) return afail(FV_BAD_ARG, "no forward run (fv_adjoint_batch_forward) to differentiate");
+  const fv_params &P = b->params;
+  const int nx = P.nx, ny = P.ny, nelem = P.array_elems, nd = b->nd;
+  const size_t bytes = 3 * b->stride * sizeof(float);
+  const int tb = 128, tg = (nd + tb - 1) / tb;
+  int wmax = 1;
+  for (int d = 0; d < nd; ++d) wmax = std::max(wmax, b->win[d].ni * b->win[d].nj);
+  const dim3 lgrid((wmax + 255) / 256, nd);
+  const dim3 bblk(kBX, kBY), bgrd((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY, nd);
+  for (int d = 0; d < nd; ++d) {
+    const AdjDesign &a = b->hdesc[d];
+    FVA_CUDA(cudaMemsetAsync(a.acc + 1, 0, 2 * size_t(nelem) * sizeof(double), b->stream));
+    FVA_CUDA(cudaMemsetAsync(&a.ctrl->rejected, 0, sizeof(a.ctrl->rejected), b->stream));
+  }
+  FVA_CUDA(cudaMemsetAsync(b->neg, 0, sizeof(int32_t) * nd, b->stream));
+  // every design takes the same number of accepted steps, so every final
+  // state is in the same buffer of its pair
+  for (int d = 0; d < nd; ++d)
+    if (b->final_cur[d] != b->final_cur[0]) return afail(FV_CUDA_ERROR, "designs end in different buffers");
+  // lambda_N: the loss gradient of the final state
+  int lc = 0;
+  for (int d = 0; d < nd; ++d) FVA_CUDA(cudaMemsetAsync(b->hdesc[d].lam[lc][0], 0, bytes, b->stream));
+  adjb_loss_grad_kernel<<<lgrid, 256, 0, b->stream>>>(b->ddesc, int(b->nsteps), -1, lc, b->final_cur[0], nx, b->stride);
+  const long long C = b->every;
+  for (long long seg0 = ((b->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
+    const long long seg1 = std::min(seg0 + C, b->nsteps);  // steps seg0+1 .. seg1
+    for (int d = 0; d < nd; ++d) {
+      const AdjDesign &a = b->hdesc[d];
+      FVA_CUDA(cudaMemcpyAsync(a.seg, a.ckpt + size_t(seg0 / C) * 3 * b->stride, bytes, cudaMemcpyDeviceToDevice,
+                               b->stream));
+    }
+    for (long long n = seg0 + 1; n <= seg1; ++n) {
+      adjb_sched_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd, int(n - 1), int(n - 1 - seg0), b->stride,
+                                                  b->fix, b->neg, b->cfl_bits);
+      const int rc = launch_b(b, true);
+      if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
+    }
+    for (long long n = seg1; n > seg0; --n) {
+      const int slot = int(n - 1 - seg0);
+      adjb_sweep_x_kernel<<<dim3(b->sweep_x_blocks, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n), slot, lc,
+                                                                              b->stride);
+      adjb_sweep_y_kernel<<<dim3(b->sweep_y_blocks, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n), slot,
+                                                                              b->sweep_y_seg, b->stride);
+      adjb_weights_kernel<<<dim3((nelem + 3) / 4, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n));
+      adjb_boundary_kernel<<<bgrd, bblk, 0, b->stream>>>(b->dp, b->ddesc, lc);
+      adjb_loss_grad_kernel<<<lgrid, 256, 0, b->stream>>>(b->ddesc, int(n - 1), slot, lc ^ 1, 0, nx, b->stride);
+      lc ^= 1;
+    }
+    FVA_CUDA(cudaGetLastError());
+  }
+  // a negative eigenvalue met by the last replay
+  adjb_sched_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd, 0, 0, b->stride, b->fix, b->neg, b->cfl_bits);
+  FVA_CUDA(cudaStreamSynchronize(b->stream));
+  std::vector<Ctrl> hc(nd);
+  FVA_CUDA(cudaMemcpy(hc.data(), b->ctrl, sizeof(Ctrl) * nd, cudaMemcpyDeviceToHost));
+  for (int d = 0; d < nd; ++d) {
+    if (hc[d].rejected != 0)
+      return afail(FV_NEGATIVE_EIGENVALUE, "a replay of design %d's recorded forward met a negative eigenvalue", d);
+    const AdjDesign &a = b->hdesc[d];
+    FVA_CUDA(cudaMemcpy(grad_amp + size_t(d) * nelem, a.acc + 1, sizeof(double) * nelem, cudaMemcpyDeviceToHost));
+    FVA_CUDA(cudaMemcpy(grad_phase + size_t(d) * nelem, a.acc + 1 + nelem, sizeof(double) * nelem,
+                        cudaMemcpyDeviceToHost));
+  }
+  // (the replays wrote only the segment buffers: the checkpoints and the
+  // final state stay, so a second backward gives the same gradients)
+  return FV_OK;
+}
+
+fv_status fv_adjoint_batch_schedule(fv_adjoint_batch *b, int32_t design, double *dt, double *T) {
+  if (!b || !dt || !T || design < 0 || design >= b->nd) return afail(FV_BAD_ARG, "bad argument");
+  if (b->h_dt[design].size() != size_t(b->nsteps)) return afail(FV_BAD_ARG, "no forward run");
+  for (long long k = 0; k < b->nsteps; ++k) {
+    dt[k] = b->h_dt[design][k];
+    T[k] = b->h_T[design][k];
+  }
   return FV_OK;
 }
 

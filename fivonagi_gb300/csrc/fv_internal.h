@@ -198,6 +198,7 @@ struct BatchInst {
   int64_t cost_begin;     // first cost unit of this instance in the batch
   int64_t cost;           // ShareCost(nx, ny).total()
   int64_t fix_base;       // first chunk id of this instance in the fix-up scratch
+  float *stages[9];       // the record launches' stage grids (batched adjoint replays)
 };
 
 // The batch's fix-up scratch has the layout of a single simulation's
@@ -228,6 +229,11 @@ int step_shape_blocks_per_sm_exact(int shape, int *warps);
 int step_shape_blocks_per_sm_fast(int shape, int *warps);
 int launch_batch_exact(const BatchArgs &a, void *stream);
 int launch_batch_fast(const BatchArgs &a, void *stream);
+// Stage-recording attempts of every instance without the finalize launch
+// (the batched adjoint's replays on frozen schedules: ghost frame, step
+// with the stage grids of BatchInst::stages, fix-up).
+int launch_batch_replay_exact(const BatchArgs &a, void *stream);
+int launch_batch_replay_fast(const BatchArgs &a, void *stream);
 int max_batch_blocks_per_sm_exact();
 int max_batch_blocks_per_sm_fast();
 

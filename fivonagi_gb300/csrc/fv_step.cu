@@ -859,6 +859,9 @@ struct BatchMarker {
 // every simulation's attempt. No CTA waits on another. Three CTAs per SM:
 // the simulation's buffers and parameters come from global memory, and at
 // four the kernel would spill (measured: three is faster).
+// STAGE -1: the attempt; kStageRecord: the attempt plus the stage grids of
+// BatchInst::stages (the batched adjoint's replays).
+template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
   // Each warp streams the (simulation, window, row) triples of an equal
   // share of the batch's cost (the simulations' ShareCost totals, end to
@@ -892,7 +895,11 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
       int shx = 0, shy = 0;
       window_shift(p, T, dt, mdx, mdy, shx, shy);
       const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
-      float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
+      float *out[STAGE == kStageRecord ? 12 : 3];
+      for (int f = 0; f < 3; ++f) out[f] = I.state[cur ^ 1][f];
+      if constexpr (STAGE == kStageRecord) {
+        for (int k2 = 0; k2 < 9; ++k2) out[3 + k2] = I.stages[k2];
+      }
       const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
       float cmax = 0.0f;
       bool neg = false;
@@ -905,8 +912,8 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
         // exact division (no fix-up work in practice), as the single-grid
         // step kernel's default: measured faster for the batch than FMA
         // division with its fix-up pass
-        stream_window<-1, PairNormalExact>(p, in, frame, out, win * kWarpCols, y0, y1, dt, T, mdx, mdy, shx, shy,
-                                           cmax, neg, mk);
+        stream_window<STAGE, PairNormalExact>(p, in, frame, out, win * kWarpCols, y0, y1, dt, T, mdx, mdy, shx, shy,
+                                              cmax, neg, mk);
         q += y1 - y0;
       }
       for (int off = 16; off > 0; off >>= 1) cmax = nanmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
@@ -928,6 +935,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_step_kernel(BatchArgs b) {
 // simulation in items of kFixItemRows rows with exact division (as
 // fixup_kernel) and folds their CFL and eigenvalue checks into the
 // simulation's atomics; batch_finalize_kernel then decides.
+template <int STAGE>
 __global__ void __launch_bounds__(kThreads, 2) batch_fixup_kernel(BatchArgs b) {
   const int lane = threadIdx.x & 31;
   constexpr unsigned kItems = kFixRows / kFixItemRows;
@@ -958,17 +966,22 @@ __global__ void __launch_bounds__(kThreads, 2) batch_fixup_kernel(BatchArgs b) {
     int shx = 0, shy = 0;
     window_shift(p, T, dt, mdx, mdy, shx, shy);
     const float *in[3] = {I.state[cur][0], I.state[cur][1], I.state[cur][2]};
-    float *out[3] = {I.state[cur ^ 1][0], I.state[cur ^ 1][1], I.state[cur ^ 1][2]};
+    float *out[STAGE == kStageRecord ? 12 : 3];
+    for (int f = 0; f < 3; ++f) out[f] = I.state[cur ^ 1][f];
+    if constexpr (STAGE == kStageRecord) {
+      for (int k2 = 0; k2 < 9; ++k2) out[3 + k2] = I.stages[k2];
+    }
     const float *frame[3] = {I.frame[0], I.frame[1], I.frame[2]};
     float cm = 0.0f;
     bool ng = false;
     FlagMarker fm;
-    stream_window<-1, PairExact, kFixPrefetch>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, fm);
+    stream_window<STAGE, PairExact, kFixPrefetch>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng,
+                                                  fm);
     if (__any_sync(0xffffffffu, fm.flagged)) {
       cm = 0.0f;
       ng = false;
       NoMarker none;
-      stream_window<-1, PairIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
+      stream_window<STAGE, PairIEEE>(p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cm, ng, none);
     }
     for (int off = 16; off > 0; off >>= 1) cm = nanmax(cm, __shfl_xor_sync(0xffffffffu, cm, off));
     const bool wneg = __any_sync(0xffffffffu, ng);
@@ -1002,15 +1015,26 @@ static int launch_batch_impl(const BatchArgs &b, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   dim3 fgrid((b.max_frame + 255) / 256, b.n);
   batch_frame_kernel<<<fgrid, 256, 0, st>>>(b);
-  batch_step_kernel<<<b.nblocks, kThreads, 0, st>>>(b);
-  batch_fixup_kernel<<<b.fix_blocks, kThreads, 0, st>>>(b);
+  batch_step_kernel<-1><<<b.nblocks, kThreads, 0, st>>>(b);
+  batch_fixup_kernel<-1><<<b.fix_blocks, kThreads, 0, st>>>(b);
   batch_finalize_kernel<<<1, 256, 0, st>>>(b);
+  return (int)cudaGetLastError();
+}
+
+// The replays of the batched adjoint: no decision (the schedule is frozen);
+// the caller resets the fix-up header and the accumulators before each one.
+static int launch_batch_replay_impl(const BatchArgs &b, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 fgrid((b.max_frame + 255) / 256, b.n);
+  batch_frame_kernel<<<fgrid, 256, 0, st>>>(b);
+  batch_step_kernel<kStageRecord><<<b.nblocks, kThreads, 0, st>>>(b);
+  batch_fixup_kernel<kStageRecord><<<b.fix_blocks, kThreads, 0, st>>>(b);
   return (int)cudaGetLastError();
 }
 
 static int batch_occupancy() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (void *)batch_step_kernel, kThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (void *)batch_step_kernel<-1>, kThreads, 0) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
 }
@@ -1078,6 +1102,7 @@ static int shape_occupancy(int shape, int &warps) {
 
 #if FV_VARIANT_EXACT
 int launch_batch_exact(const BatchArgs &a, void *stream) { return exact_ns::launch_batch_impl(a, stream); }
+int launch_batch_replay_exact(const BatchArgs &a, void *stream) { return exact_ns::launch_batch_replay_impl(a, stream); }
 int max_batch_blocks_per_sm_exact() { return exact_ns::batch_occupancy(); }
 int launch_step_exact(const StepArgs &a, int warps, int stage, void *stream) {
   return warps == exact_ns::kWarps ? exact_ns::launch_impl(a, stage, stream)
@@ -1089,6 +1114,7 @@ int max_blocks_per_sm_exact(int warps, int stage) {
 int step_shape_blocks_per_sm_exact(int shape, int *warps) { return exact_ns::shape_occupancy(shape, *warps); }
 #else
 int launch_batch_fast(const BatchArgs &a, void *stream) { return fast_ns::launch_batch_impl(a, stream); }
+int launch_batch_replay_fast(const BatchArgs &a, void *stream) { return fast_ns::launch_batch_replay_impl(a, stream); }
 int max_batch_blocks_per_sm_fast() { return fast_ns::batch_occupancy(); }
 int launch_step_fast(const StepArgs &a, int warps, int stage, void *stream) {
   return warps == fast_ns::kWarps ? fast_ns::launch_impl(a, stage, stream)

@@ -373,6 +373,26 @@ fv_status fv_batch_time_run(fv_batch *b, int64_t nattempts, float *ms);
 fv_status fv_batch_set_launch(fv_batch *b, int32_t blocks);
 fv_status fv_batch_get_launch(fv_batch *b, int32_t *blocks, int32_t *max_resident);
 
+/* ------------------------------------------------------ batched adjoint
+ * D designs of one grid and one set of physical parameters (fv_params of
+ * the phased array), each with its own element weights, loss window
+ * (windows[d]) and adaptive dt schedule, stepped together: every attempt of
+ * the recorded forward, every replayed step and every reverse step of the
+ * backward is one launch sequence over all D designs. Each design's loss
+ * and gradients equal what fv_adjoint_forward/backward give for it alone,
+ * bit for bit. Memory: D times fv_adjoint's. amp, phase: D x array_elems,
+ * design-major; loss: D; grad_amp, grad_phase: D x array_elems. No
+ * reference counterpart (the reference has no adjoint). */
+typedef struct fv_adjoint_batch fv_adjoint_batch;
+fv_status fv_adjoint_batch_create(const fv_params *p, int32_t ndesigns, const fv_loss_window *windows,
+                                  int64_t nsteps, int32_t checkpoint_every, fv_adjoint_batch **out);
+fv_status fv_adjoint_batch_destroy(fv_adjoint_batch *b);
+fv_status fv_adjoint_batch_set_stream(fv_adjoint_batch *b, void *cuda_stream);
+fv_status fv_adjoint_batch_forward(fv_adjoint_batch *b, const float *amp, const float *phase, double *loss);
+fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, double *grad_phase);
+/* design's recorded dt and T (before each accepted step), nsteps each */
+fv_status fv_adjoint_batch_schedule(fv_adjoint_batch *b, int32_t design, double *dt, double *T);
+
 /* ------------------------------------------------- step without allocation
  * For callers that cannot let this library call cudaMalloc: programs whose
  * device memory belongs to one allocator of their own (a framework's

@@ -176,3 +176,34 @@ def test_backward_repeats_and_keeps_the_final_state():
     assert np.array_equal(ga1, ga2) and np.array_equal(gp1, gp2)
     adj.close()
 
+
+
+def test_batched_adjoint_equals_each_design_alone():
+    """Three designs (own weights, own loss windows) through one
+    fv_adjoint_batch: every loss, schedule and gradient equals the
+    single-design adjoint's for that design, bit for bit, on two backward
+    passes."""
+    from fivonagi_gb300.adjoint import AdjointBatch
+
+    p = _params()
+    wins = [loss_window(14, 18, 8, 8, 60, NSTEPS), loss_window(30, 10, 6, 10, 40, NSTEPS - 10),
+            loss_window(40, 30, 10, 6, 90, NSTEPS)]
+    weights = [array_weights(p.array_elems, 20 + d, p.ampl) for d in range(3)]
+    amp = np.stack([w[0] for w in weights])
+    ph = np.stack([w[1] for w in weights])
+    ab = AdjointBatch(p, wins, NSTEPS, checkpoint_every=16)
+    losses = ab.forward(amp, ph)
+    ga, gp = ab.backward()
+    ga2, gp2 = ab.backward()
+    assert np.array_equal(ga, ga2) and np.array_equal(gp, gp2)
+    for d in range(3):
+        adj = Adjoint(p, wins[d], NSTEPS, checkpoint_every=16)
+        loss = adj.forward(amp[d], ph[d])
+        g1, g2 = adj.backward()
+        dts, Ts = adj.schedule()
+        bdts, bTs = ab.schedule(d)
+        adj.close()
+        assert loss == losses[d]
+        assert np.array_equal(dts, bdts) and np.array_equal(Ts, bTs)
+        assert np.array_equal(g1, ga[d]) and np.array_equal(g2, gp[d]), d
+    ab.close()
