@@ -563,6 +563,15 @@ struct AdjDesign {
   long long first, last;
 };
 
+// Up to kDesignsPerLaunch designs' descriptors by value, as a kernel
+// parameter: parameter space cannot alias the kernels' stores, so the
+// compiler re-reads the buffers' addresses from it where a descriptor in
+// global memory would hold them in registers through the sweeps' loops.
+constexpr int kDesignsPerLaunch = 16;
+struct AdjDesignSet {
+  AdjDesign d[kDesignsPerLaunch];
+};
+
 __device__ __forceinline__ CG3 cstate(const float *base, size_t stride, long long k) {
   return CG3{{base + (size_t(k) * 3 + 0) * stride, base + (size_t(k) * 3 + 1) * stride,
               base + (size_t(k) * 3 + 2) * stride}};
@@ -606,9 +615,9 @@ __global__ void adjb_reset_kernel(const AdjDesign *D, int nd, float dt, float T,
 }
 
 // The record launch of a batched forward attempt (record_body per design).
-__global__ void adjb_record_kernel(const AdjDesign *D, int parity, int nsteps, size_t stride, size_t ncell,
-                                   int every, int nx) {
-  const AdjDesign &a = D[blockIdx.y];
+__global__ void adjb_record_kernel(const __grid_constant__ AdjDesignSet D, int parity, int nsteps, size_t stride,
+                                   size_t ncell, int every, int nx) {
+  const AdjDesign &a = D.d[blockIdx.y];
   record_body(a.ctrl, a.rec, parity, a.sched_dt, a.sched_T, nsteps, gg(a.state[0]), gg(a.state[1]), a.ckpt, stride,
               ncell, every, nx, a.i0, a.j0, a.ni, a.nj, a.first, a.last, a.acc);
 }
@@ -661,37 +670,37 @@ __global__ void adjb_forward_inst_kernel(const AdjDesign *D, BatchInst *inst, in
 
 // Reverse step n (input u_{n-1}, segment slot `slot`): diffusion and x sweep,
 // lam[lc] -> tmp[1].
-__global__ void __launch_bounds__(128) adjb_sweep_x_kernel(DevParams p, const AdjDesign *D, int n, int slot,
-                                                           int lc, size_t stride) {
-  const AdjDesign &a = D[blockIdx.y];
+__global__ void __launch_bounds__(128) adjb_sweep_x_kernel(DevParams p, const __grid_constant__ AdjDesignSet D,
+                                                           int n, int slot, int lc, size_t stride) {
+  const AdjDesign &a = D.d[blockIdx.y];
   sweep_x_body(p, a.sched_dt[n - 1], cstage(a.stg, stride, slot, 1), cstage(a.stg, stride, slot, 2), cg(a.lam[lc]),
                gg(a.tmp[1]));
 }
 
 // y sweep: tmp[1] -> tmp[0].
-__global__ void __launch_bounds__(128) adjb_sweep_y_kernel(DevParams p, const AdjDesign *D, int n, int slot,
-                                                           int seg, size_t stride) {
-  const AdjDesign &a = D[blockIdx.y];
+__global__ void __launch_bounds__(128) adjb_sweep_y_kernel(DevParams p, const __grid_constant__ AdjDesignSet D,
+                                                           int n, int slot, int seg, size_t stride) {
+  const AdjDesign &a = D.d[blockIdx.y];
   sweep_y_body(p, a.sched_dt[n - 1], cstage(a.stg, stride, slot, 0), cg(a.tmp[1]), gg(a.tmp[0]), seg);
 }
 
-__global__ void adjb_weights_kernel(DevParams p, const AdjDesign *D, int n) {
-  const AdjDesign &a = D[blockIdx.y];
+__global__ void adjb_weights_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int n) {
+  const AdjDesign &a = D.d[blockIdx.y];
   weights_body(p, a.weights, a.sched_T[n - 1], cg(a.tmp[0]), a.acc + 1, a.acc + 1 + p.nelem);
 }
 
 // boundary: tmp[0] -> lam[lc ^ 1]
-__global__ void adjb_boundary_kernel(DevParams p, const AdjDesign *D, int lc) {
-  const AdjDesign &a = D[blockIdx.z];
+__global__ void adjb_boundary_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int lc) {
+  const AdjDesign &a = D.d[blockIdx.z];
   boundary_body(p, cg(a.tmp[0]), gg(a.lam[lc ^ 1]));
 }
 
 // The loss gradient of the state after accepted step m (segment slot
 // `slot`, or the final forward state when slot < 0) into lam[lc], for the
 // designs whose loss steps include m.
-__global__ void adjb_loss_grad_kernel(const AdjDesign *D, int m, int slot, int lc, int final_cur, int nx,
-                                      size_t stride) {
-  const AdjDesign &a = D[blockIdx.y];
+__global__ void adjb_loss_grad_kernel(const __grid_constant__ AdjDesignSet D, int m, int slot, int lc, int final_cur,
+                                      int nx, size_t stride) {
+  const AdjDesign &a = D.d[blockIdx.y];
   if (m < a.first || m > a.last) return;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.ni * a.nj) return;
@@ -740,7 +749,7 @@ struct fv_adjoint {
   int final_cur = 0;           // state[final_cur] holds the last forward's final state
                                // (the backward's replays reuse the control block)
   int exact = 1;
-  AdjDesign *desc = nullptr;   // this design's buffers for the reverse kernels (device, one entry)
+  AdjDesignSet desc{};         // this design's buffers for the reverse kernels (entry 0)
 };
 
 namespace {
@@ -988,9 +997,7 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
     d.nj = w->nj;
     d.first = w->step_first;
     d.last = w->step_last;
-    e = cudaMalloc(&a->desc, sizeof(AdjDesign));
-    if (e == cudaSuccess) e = cudaMemcpy(a->desc, &d, sizeof(AdjDesign), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "adjoint descriptor: %s", cudaGetErrorString(e)));
+    a->desc.d[0] = d;
   }
   *out = a;
   return FV_OK;
@@ -1008,7 +1015,6 @@ fv_status fv_adjoint_destroy(fv_adjoint *a) {
   if (a->fix) cudaFree(a->fix);
   if (a->sched) cudaFree(a->sched);
   if (a->acc) cudaFree(a->acc);
-  if (a->desc) cudaFree(a->desc);
   if (a->own_stream) cudaStreamDestroy(a->own_stream);
   delete a;
   return FV_OK;
@@ -1151,7 +1157,8 @@ struct fv_adjoint_batch {
   std::vector<fv_loss_window> win;
   std::vector<float *> mem;     // per design: all grids
   std::vector<AdjDesign> hdesc;
-  AdjDesign *ddesc = nullptr;
+  AdjDesign *ddesc = nullptr;   // device copy (the control-block kernels)
+  std::vector<AdjDesignSet> sets;  // by value, kDesignsPerLaunch designs a launch (the reverse kernels)
   float *small = nullptr;       // weights, schedules of every design
   double *acc = nullptr;        // per design: 1 + 2 nelem
   Ctrl *ctrl = nullptr;         // per design
@@ -1172,6 +1179,11 @@ struct fv_adjoint_batch {
 };
 
 namespace {
+
+// designs in group g of the batch's descriptor sets
+int group_size(const fv_adjoint_batch *b, size_t g) {
+  return std::min(kDesignsPerLaunch, b->nd - int(g) * kDesignsPerLaunch);
+}
 
 int launch_b(const fv_adjoint_batch *b, bool replay) {
   if (replay) return b->exact ? launch_batch_replay_exact(b->args, b->stream) : launch_batch_replay_fast(b->args, b->stream);
@@ -1312,6 +1324,11 @@ fv_status fv_adjoint_batch_create(const fv_params *p, int32_t ndesigns, const fv
   e = cudaMalloc(&b->fix, b->fix_words * sizeof(uint32_t));
   if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "cudaMalloc fix-up scratch: %s", cudaGetErrorString(e)));
   FVA_CUDA(cudaMemcpyAsync(b->ddesc, b->hdesc.data(), sizeof(AdjDesign) * ndesigns, cudaMemcpyHostToDevice, b->stream));
+  for (int g0 = 0; g0 < ndesigns; g0 += kDesignsPerLaunch) {
+    AdjDesignSet set{};
+    for (int k = 0; k < kDesignsPerLaunch && g0 + k < ndesigns; ++k) set.d[k] = b->hdesc[g0 + k];
+    b->sets.push_back(set);
+  }
   FVA_CUDA(cudaMemcpyAsync(b->inst, b->hinst.data(), sizeof(BatchInst) * ndesigns, cudaMemcpyHostToDevice, b->stream));
   FVA_CUDA(cudaMemsetAsync(b->fix, 0, b->fix_words * sizeof(uint32_t), b->stream));
   FVA_CUDA(cudaMemsetAsync(b->cfl_bits, 0, sizeof(uint32_t) * ndesigns, b->stream));
@@ -1348,12 +1365,13 @@ fv_status fv_adjoint_batch_create(const fv_params *p, int32_t ndesigns, const fv
     // the y sweep's row segments as for one design; the CTAs of both sweeps
     // are spread over the designs (gridDim.y)
     const long long xwarps = (long long)windows_x * p->ny;
-    b->sweep_x_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)ox * b->sms / ndesigns), (xwarps + 3) / 4)));
+    const long long per_launch = std::min(ndesigns, kDesignsPerLaunch);
+    b->sweep_x_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)ox * b->sms / per_launch), (xwarps + 3) / 4)));
     const long long strips = (p->nx + 31) / 32, ywarps = 4LL * oy * b->sms;
     const long long nseg = std::max(1LL, std::min((long long)(p->ny + 15) / 16, ywarps / strips));
     b->sweep_y_seg = int((p->ny + nseg - 1) / nseg);
     const long long ytotal = strips * ((p->ny + b->sweep_y_seg - 1) / b->sweep_y_seg);
-    b->sweep_y_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)oy * b->sms / ndesigns), (ytotal + 3) / 4)));
+    b->sweep_y_blocks = int(std::max(1LL, std::min(std::max(1LL, (long long)oy * b->sms / per_launch), (ytotal + 3) / 4)));
   }
   e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return cleanup(afail(FV_CUDA_ERROR, "adjoint batch set-up: %s", cudaGetErrorString(e)));
@@ -1410,15 +1428,17 @@ fv_status fv_adjoint_batch_forward(fv_adjoint_batch *b, const float *amp, const 
   adjb_forward_inst_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd);
   adjb_reset_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, nd, float(P.dtini), -float(P.tide), b->nsteps);
   FVA_CUDA(cudaGetLastError());
-  const dim3 rgrid(std::max(1, b->sms * 4 / nd), nd);
+  const int rx = std::max(1, b->sms * 4 / nd);
   std::vector<Ctrl> hc(nd);
   long long todo = b->nsteps, attempt = 0;
   for (int round = 0; round < 64 && todo > 0; ++round) {
     for (long long k = 0; k < todo; ++k, ++attempt) {
       const int rc = launch_b(b, false);
       if (rc != 0) return afail(FV_CUDA_ERROR, "batch step launch: %s", cudaGetErrorString((cudaError_t)rc));
-      adjb_record_kernel<<<rgrid, 256, 0, b->stream>>>(b->ddesc, int(attempt & 1), int(b->nsteps), b->stride,
-                                                        b->ncell, b->every, P.nx);
+      for (size_t g = 0; g < b->sets.size(); ++g)
+        adjb_record_kernel<<<dim3(rx, group_size(b, g)), 256, 0, b->stream>>>(b->sets[g], int(attempt & 1),
+                                                                             int(b->nsteps), b->stride, b->ncell,
+                                                                             b->every, P.nx);
     }
     FVA_CUDA(cudaGetLastError());
     FVA_CUDA(cudaMemcpyAsync(hc.data(), b->ctrl, sizeof(Ctrl) * nd, cudaMemcpyDeviceToHost, b->stream));
@@ -1455,8 +1475,8 @@ fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, doubl
   const int tb = 128, tg = (nd + tb - 1) / tb;
   int wmax = 1;
   for (int d = 0; d < nd; ++d) wmax = std::max(wmax, b->win[d].ni * b->win[d].nj);
-  const dim3 lgrid((wmax + 255) / 256, nd);
-  const dim3 bblk(kBX, kBY), bgrd((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY, nd);
+  const int lx = (wmax + 255) / 256;
+  const dim3 bblk(kBX, kBY);
   for (int d = 0; d < nd; ++d) {
     const AdjDesign &a = b->hdesc[d];
     FVA_CUDA(cudaMemsetAsync(a.acc + 1, 0, 2 * size_t(nelem) * sizeof(double), b->stream));
@@ -1470,7 +1490,9 @@ fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, doubl
   // lambda_N: the loss gradient of the final state
   int lc = 0;
   for (int d = 0; d < nd; ++d) FVA_CUDA(cudaMemsetAsync(b->hdesc[d].lam[lc][0], 0, bytes, b->stream));
-  adjb_loss_grad_kernel<<<lgrid, 256, 0, b->stream>>>(b->ddesc, int(b->nsteps), -1, lc, b->final_cur[0], nx, b->stride);
+  for (size_t g = 0; g < b->sets.size(); ++g)
+    adjb_loss_grad_kernel<<<dim3(lx, group_size(b, g)), 256, 0, b->stream>>>(b->sets[g], int(b->nsteps), -1, lc,
+                                                                             b->final_cur[0], nx, b->stride);
   const long long C = b->every;
   for (long long seg0 = ((b->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, b->nsteps);  // steps seg0+1 .. seg1
@@ -1487,13 +1509,18 @@ fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, doubl
     }
     for (long long n = seg1; n > seg0; --n) {
       const int slot = int(n - 1 - seg0);
-      adjb_sweep_x_kernel<<<dim3(b->sweep_x_blocks, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n), slot, lc,
-                                                                              b->stride);
-      adjb_sweep_y_kernel<<<dim3(b->sweep_y_blocks, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n), slot,
-                                                                              b->sweep_y_seg, b->stride);
-      adjb_weights_kernel<<<dim3((nelem + 3) / 4, nd), 128, 0, b->stream>>>(b->dp, b->ddesc, int(n));
-      adjb_boundary_kernel<<<bgrd, bblk, 0, b->stream>>>(b->dp, b->ddesc, lc);
-      adjb_loss_grad_kernel<<<lgrid, 256, 0, b->stream>>>(b->ddesc, int(n - 1), slot, lc ^ 1, 0, nx, b->stride);
+      for (size_t g = 0; g < b->sets.size(); ++g) {
+        const AdjDesignSet &S = b->sets[g];
+        const int gn = group_size(b, g);
+        adjb_sweep_x_kernel<<<dim3(b->sweep_x_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot, lc,
+                                                                                b->stride);
+        adjb_sweep_y_kernel<<<dim3(b->sweep_y_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot,
+                                                                                b->sweep_y_seg, b->stride);
+        adjb_weights_kernel<<<dim3((nelem + 3) / 4, gn), 128, 0, b->stream>>>(b->dp, S, int(n));
+        adjb_boundary_kernel<<<dim3((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY, gn), bblk, 0, b->stream>>>(b->dp, S,
+                                                                                                       lc);
+        adjb_loss_grad_kernel<<<dim3(lx, gn), 256, 0, b->stream>>>(S, int(n - 1), slot, lc ^ 1, 0, nx, b->stride);
+      }
       lc ^= 1;
     }
     FVA_CUDA(cudaGetLastError());
