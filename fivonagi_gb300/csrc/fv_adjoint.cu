@@ -78,6 +78,112 @@ fv_status afail(fv_status s, const char *fmt, ...) {
     if (e_ != cudaSuccess) return afail(FV_CUDA_ERROR, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// Issues one backward segment's launches (`issue`, returning a status)
+// captured as a CUDA graph on `st` and launches the graph: the first
+// capture is instantiated into `exec`, later ones update it in place (every
+// full segment has the same launches with other arguments), with a new
+// instantiation when the shape differs (the short segment at the end of the
+// run). A stream that cannot be captured (the legacy default stream) gets
+// the launches directly.
+template <class F>
+fv_status run_captured(cudaStream_t st, cudaGraphExec_t &exec, F &&issue) {
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return issue();
+  }
+  const fv_status s = issue();
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (s != FV_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return s != FV_OK ? s : afail(FV_CUDA_ERROR, "segment capture: %s", cudaGetErrorString(e));
+  }
+  if (exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(exec, g, &info) != cudaSuccess) {
+      cudaGetLastError();  // a different shape: instantiate anew
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+  }
+  if (!exec) e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return afail(FV_CUDA_ERROR, "segment graph: %s", cudaGetErrorString(e));
+  e = cudaGraphLaunch(exec, st);
+  if (e != cudaSuccess) return afail(FV_CUDA_ERROR, "segment graph launch: %s", cudaGetErrorString(e));
+  return FV_OK;
+}
+
+// The recorded forward's attempts in graphs of kRecordGraphAttempts (even:
+// the record launch alternates between two slots by attempt parity), each
+// captured once per handle (the launches' arguments do not change).
+constexpr int kRecordGraphAttempts = 32;
+// Issues n attempts (`attempt(k)` for k = first .. first + n - 1), the even-
+// aligned whole chunks of them through the cached graph `g` (captured on
+// first use; a stream that cannot be captured gets the launches directly).
+template <class F>
+fv_status run_attempts(cudaStream_t st, cudaGraphExec_t &g, long long first, long long n, F &&attempt) {
+  long long k = first, end = first + n;
+  if (n >= kRecordGraphAttempts + 1 || (n >= kRecordGraphAttempts && (first & 1) == 0)) {
+    if (k & 1) {
+      const fv_status s = attempt(k++);
+      if (s != FV_OK) return s;
+    }
+    if (!g && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      fv_status s = FV_OK;
+      for (long long j = 0; j < kRecordGraphAttempts && s == FV_OK; ++j) s = attempt(j);
+      cudaGraph_t cg = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(st, &cg);
+      if (s == FV_OK && e == cudaSuccess && cudaGraphInstantiate(&g, cg, 0) != cudaSuccess) g = nullptr;
+      if (cg) cudaGraphDestroy(cg);
+      if (s != FV_OK) return s;
+      if (e != cudaSuccess || !g) return afail(FV_CUDA_ERROR, "forward graph: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    cudaGetLastError();
+    if (g) {
+      for (; end - k >= kRecordGraphAttempts; k += kRecordGraphAttempts) {
+        const cudaError_t e = cudaGraphLaunch(g, st);
+        if (e != cudaSuccess) return afail(FV_CUDA_ERROR, "forward graph launch: %s", cudaGetErrorString(e));
+      }
+    }
+  }
+  for (; k < end; ++k) {
+    const fv_status s = attempt(k);
+    if (s != FV_OK) return s;
+  }
+  return FV_OK;
+}
+
+// A side stream and two events: launches between fork() and join() run on
+// the side stream, concurrently with what the main stream does meanwhile
+// (inside a capture they become a parallel branch of the graph).
+struct Fork {
+  cudaStream_t side = nullptr;
+  cudaEvent_t go = nullptr, done = nullptr;
+  cudaError_t init() {
+    if (side) return cudaSuccess;
+    cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&go, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    return e;
+  }
+  cudaError_t fork(cudaStream_t main) {
+    cudaError_t e = cudaEventRecord(go, main);
+    return e == cudaSuccess ? cudaStreamWaitEvent(side, go, 0) : e;
+  }
+  cudaError_t join(cudaStream_t main) {
+    cudaError_t e = cudaEventRecord(done, side);
+    return e == cudaSuccess ? cudaStreamWaitEvent(main, done, 0) : e;
+  }
+  void release() {
+    if (go) cudaEventDestroy(go);
+    if (done) cudaEventDestroy(done);
+    if (side) cudaStreamDestroy(side);
+    side = nullptr;
+    go = done = nullptr;
+  }
+};
+
 __device__ __forceinline__ bool interior(const DevParams &p, int i, int j) {
   return i >= 2 && i <= p.nx - 3 && j >= 2 && j <= p.ny - 3;
 }
@@ -477,7 +583,14 @@ __device__ __forceinline__ bool array_row(const DevParams &p, int j) {
 // (right column pair, top and bottom row pairs, left pair outside the
 // array), zeros (corners) or the source (left pair on the array's rows).
 // The copies' adjoints return to the cells they copy.
-__device__ __forceinline__ void boundary_body(const DevParams &p, const CG3 &lb, const G3 &lp) {
+// `loss`: the loss gradient of the state u1 after the step's input (a
+// window of the design's loss, or none) added to the output's u1 adjoint.
+struct LossTerm {
+  const float *u1;  // nullptr: the step is outside the loss steps
+  int i0, j0, ni, nj;
+  float coef;
+};
+__device__ __forceinline__ void boundary_body(const DevParams &p, const CG3 &lb, const G3 &lp, const LossTerm &loss) {
   const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
   const int nx = p.nx, ny = p.ny;
   if (i >= nx || j >= ny) return;
@@ -494,6 +607,8 @@ __device__ __forceinline__ void boundary_body(const DevParams &p, const CG3 &lb,
     if (j == 2) { add(i, 0); add(i, 1); }
     if (i == 2 && !array_row(p, j)) { add(0, j); add(1, j); }
   }
+  if (loss.u1 && i >= loss.i0 && i < loss.i0 + loss.ni && j >= loss.j0 && j < loss.j0 + loss.nj)
+    a[0] += 2.0f * loss.u1[o] * loss.coef;
   lp.f[0][o] = a[0];
   lp.f[1][o] = a[1];
   lp.f[2][o] = a[2];
@@ -505,9 +620,7 @@ __device__ __forceinline__ void boundary_body(const DevParams &p, const CG3 &lb,
 // (a strided loop when an element spans more than 16 rows), a warp
 // reduction in FP64 sums them, and lane 0 updates the element's sums.
 __device__ __forceinline__ void weights_body(const DevParams &p, const float *weights, float T, const CG3 &lb,
-                                             double *g_amp, double *g_ph) {
-  const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
+                                             double *g_amp, double *g_ph, int e, int lane) {
   if (e >= p.nelem) return;  // warp-uniform
   const float amp = weights[e], ph = weights[p.nelem + e];
   const float ramp = gmin(gmax(T * p.ramp, 0.0f), 1.0f);
@@ -561,6 +674,7 @@ struct AdjDesign {
   AdjRec *rec;                // two slots, by attempt parity
   int i0, j0, ni, nj;
   long long first, last;
+  float loss_coef;            // 1 / (loss steps x window cells), rounded once
 };
 
 // Up to kDesignsPerLaunch designs' descriptors by value, as a kernel
@@ -684,15 +798,26 @@ __global__ void __launch_bounds__(128) adjb_sweep_y_kernel(DevParams p, const __
   sweep_y_body(p, a.sched_dt[n - 1], cstage(a.stg, stride, slot, 0), cg(a.tmp[1]), gg(a.tmp[0]), seg);
 }
 
-__global__ void adjb_weights_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int n) {
+// Weight gradients of reverse step n from tmp[0] (a warp per element).
+__global__ void __launch_bounds__(128) adjb_weights_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int n) {
   const AdjDesign &a = D.d[blockIdx.y];
-  weights_body(p, a.weights, a.sched_T[n - 1], cg(a.tmp[0]), a.acc + 1, a.acc + 1 + p.nelem);
+  weights_body(p, a.weights, a.sched_T[n - 1], cg(a.tmp[0]), a.acc + 1, a.acc + 1 + p.nelem,
+               (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), (int)(threadIdx.x & 31));
 }
 
-// boundary: tmp[0] -> lam[lc ^ 1]
-__global__ void adjb_boundary_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int lc) {
+// The boundary reverse of step n (input u_{n-1}, segment slot `slot`):
+// tmp[0] -> lam[lc ^ 1], with the loss gradient of u_{n-1} added where the
+// step is among the loss steps.
+__global__ void adjb_boundary_kernel(DevParams p, const __grid_constant__ AdjDesignSet D, int n, int slot, int lc,
+                                     size_t stride) {
   const AdjDesign &a = D.d[blockIdx.z];
-  boundary_body(p, cg(a.tmp[0]), gg(a.lam[lc ^ 1]));
+  const long long m = n - 1;  // the loss of the state after accepted step m
+  LossTerm loss{nullptr, a.i0, a.j0, a.ni, a.nj, 0.0f};
+  if (m >= a.first && m <= a.last) {
+    loss.u1 = a.seg + size_t(slot) * 3 * stride;
+    loss.coef = a.loss_coef;
+  }
+  boundary_body(p, cg(a.tmp[0]), gg(a.lam[lc ^ 1]), loss);
 }
 
 // The loss gradient of the state after accepted step m (segment slot
@@ -704,7 +829,7 @@ __global__ void adjb_loss_grad_kernel(const __grid_constant__ AdjDesignSet D, in
   if (m < a.first || m > a.last) return;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.ni * a.nj) return;
-  const float coef = float(1.0 / (double(a.last - a.first + 1) * double(a.ni) * double(a.nj)));
+  const float coef = a.loss_coef;
   const float *u1 = slot < 0 ? a.state[final_cur][0] : a.seg + size_t(slot) * 3 * stride;
   const size_t o = size_t(a.i0 + k % a.ni) + size_t(a.j0 + k / a.ni) * nx;
   a.lam[lc][0][o] += 2.0f * u1[o] * coef;
@@ -713,6 +838,12 @@ __global__ void adjb_loss_grad_kernel(const __grid_constant__ AdjDesignSet D, in
 }  // namespace
 
 // ------------------------------------------------------------------ handle
+
+// The loss's weight of one window cell and step (the device kernels read
+// it from the descriptor: an FP64 division per thread is slow on this GPU).
+static float loss_coef(const fv_loss_window &w) {
+  return float(1.0 / (double(w.step_last - w.step_first + 1) * double(w.ni) * double(w.nj)));
+}
 
 struct fv_adjoint {
   fv_params params{};
@@ -724,6 +855,9 @@ struct fv_adjoint {
   int sms = 0, max_resident = 0;
   size_t ncell = 0, stride = 0;
   cudaStream_t stream = nullptr, own_stream = nullptr;
+  cudaGraphExec_t seg_graph = nullptr;  // the backward's segment graph
+  cudaGraphExec_t rec_graph = nullptr;  // the recorded forward's attempts
+  Fork fork;                            // the weights' branch of a reverse step
   // device memory: one allocation of grids, plus small arrays
   float *mem = nullptr;
   float *state[2][3] = {};      // forward state pair
@@ -779,7 +913,6 @@ int launch(const fv_adjoint *a, const StepArgs &s, int stage) {
 }
 
 G3 g3(float *const f[3]) { return G3{{f[0], f[1], f[2]}}; }
-CG3 cg3(float *const f[3]) { return CG3{{f[0], f[1], f[2]}}; }
 
 float *slot(float *base, size_t stride, long long k, int f) { return base + (size_t(k) * 3 + f) * stride; }
 // grid f of stage st (0 = B, 1 = S1, 2 = S2) of the segment's k-th step
@@ -814,13 +947,17 @@ fv_status run_forward(fv_adjoint *a, bool record, double *loss) {
     long long todo = a->nsteps;
     long long attempt = 0;
     adj_pre_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->rec);  // the scalars before attempt 0
+    auto one = [&](long long k) -> fv_status {
+      const int rc = launch(a, s, -1);
+      if (rc != 0) return afail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
+      adjb_record_kernel<<<dim3(cgrid, 1), 256, 0, a->stream>>>(a->desc, int(k & 1), int(a->nsteps), a->stride,
+                                                                a->ncell, a->every, P.nx);
+      return FV_OK;
+    };
     for (int round = 0; round < 64 && todo > 0; ++round) {
-      for (long long k = 0; k < todo; ++k, ++attempt) {
-        int rc = launch(a, s, -1);
-        if (rc != 0) return afail(FV_CUDA_ERROR, "step launch: %s", cudaGetErrorString((cudaError_t)rc));
-        adjb_record_kernel<<<dim3(cgrid, 1), 256, 0, a->stream>>>(a->desc, int(attempt & 1), int(a->nsteps),
-                                                                  a->stride, a->ncell, a->every, P.nx);
-      }
+      const fv_status rs = run_attempts(a->stream, a->rec_graph, attempt, todo, one);
+      if (rs != FV_OK) return rs;
+      attempt += todo;
       FVA_CUDA(cudaGetLastError());
       Ctrl c;
       FVA_CUDA(cudaMemcpyAsync(&c, a->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, a->stream));
@@ -997,6 +1134,7 @@ fv_status fv_adjoint_create(const fv_params *p, const fv_loss_window *w, int64_t
     d.nj = w->nj;
     d.first = w->step_first;
     d.last = w->step_last;
+    d.loss_coef = loss_coef(*w);
     a->desc.d[0] = d;
   }
   *out = a;
@@ -1015,6 +1153,9 @@ fv_status fv_adjoint_destroy(fv_adjoint *a) {
   if (a->fix) cudaFree(a->fix);
   if (a->sched) cudaFree(a->sched);
   if (a->acc) cudaFree(a->acc);
+  if (a->seg_graph) cudaGraphExecDestroy(a->seg_graph);
+  if (a->rec_graph) cudaGraphExecDestroy(a->rec_graph);
+  a->fork.release();
   if (a->own_stream) cudaStreamDestroy(a->own_stream);
   delete a;
   return FV_OK;
@@ -1073,6 +1214,7 @@ fv_status fv_adjoint_get_state(fv_adjoint *a, float *u1, float *u2, float *u3) {
 fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phase) {
   if (!a || !grad_amp || !grad_phase) return afail(FV_BAD_ARG, "NULL argument");
   if (!a->have_forward) return afail(FV_BAD_ARG, "no forward run (fv_adjoint_forward) to differentiate");
+  FVA_CUDA(a->fork.init());
   const fv_params &P = a->params;
   const int nx = P.nx, ny = P.ny, nelem = P.array_elems;
   const fv_loss_window &w = a->win;
@@ -1093,42 +1235,49 @@ fv_status fv_adjoint_backward(fv_adjoint *a, double *grad_amp, double *grad_phas
   const long long C = a->every;
   for (long long seg0 = ((a->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, a->nsteps);  // steps seg0+1 .. seg1
-    // the segment's states u_seg0 .. u_seg1 and the stage grids of steps
-    // seg0+1 .. seg1: checkpoint, then replay with stage recording
-    FVA_CUDA(cudaMemcpyAsync(slot(a->seg, a->stride, 0, 0), slot(a->ckpt, a->stride, seg0 / C, 0), bytes,
-                             cudaMemcpyDeviceToDevice, a->stream));
-    for (long long n = seg0 + 1; n <= seg1; ++n) {
-      float *in[3], *out[3];
-      for (int f = 0; f < 3; ++f) {
-        in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
-        out[f] = slot(a->seg, a->stride, n - seg0, f);
+    const fv_status rs = run_captured(a->stream, a->seg_graph, [&]() -> fv_status {
+      // the segment's states u_seg0 .. u_seg1 and the stage grids of steps
+      // seg0+1 .. seg1: checkpoint, then replay with stage recording
+      FVA_CUDA(cudaMemcpyAsync(slot(a->seg, a->stride, 0, 0), slot(a->ckpt, a->stride, seg0 / C, 0), bytes,
+                               cudaMemcpyDeviceToDevice, a->stream));
+      for (long long n = seg0 + 1; n <= seg1; ++n) {
+        float *in[3], *out[3];
+        for (int f = 0; f < 3; ++f) {
+          in[f] = slot(a->seg, a->stride, n - 1 - seg0, f);
+          out[f] = slot(a->seg, a->stride, n - seg0, f);
+        }
+        adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0, a->fix);
+        StepArgs s = step_args(a, a->dp_replay, in, out);
+        for (int st = 0; st < 3; ++st)
+          for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = stage_grid(a, n - 1 - seg0, st, f);
+        const int rc = launch(a, s, kStageReplay);
+        if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
       }
-      adj_sched_kernel<<<1, 1, 0, a->stream>>>(a->ctrl, a->sched, a->sched + a->nsteps, int(n - 1), 0, a->fix);
-      StepArgs s = step_args(a, a->dp_replay, in, out);
-      for (int st = 0; st < 3; ++st)
-        for (int f = 0; f < 3; ++f) s.stages[3 * st + f] = stage_grid(a, n - 1 - seg0, st, f);
-      const int rc = launch(a, s, kStageReplay);
-      if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
-    }
-    for (long long n = seg1; n > seg0; --n) {
-      // reverse of step n, whose input is u_{n-1} (segment slot n-1-seg0;
-      // its recorded boundary-applied, y-swept and x-swept states are the
-      // slot's stage grids)
-      const int slot = int(n - 1 - seg0);
-      // diffusion (on S2) and x sweep (on S1): lam[lc] -> tmp1 (adjoint of S1)
-      adjb_sweep_x_kernel<<<dim3(a->sweep_x_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot, lc,
-                                                                             a->stride);
-      // y sweep on B: tmp1 -> tmp0 (adjoint of B)
-      adjb_sweep_y_kernel<<<dim3(a->sweep_y_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot,
-                                                                             a->sweep_y_seg, a->stride);
-      // boundary: weights, then lam[lc ^ 1] = lam_{n-1}
-      adjb_weights_kernel<<<dim3((nelem + 3) / 4, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n));
-      adjb_boundary_kernel<<<dim3(grd.x, grd.y, 1), blk, 0, a->stream>>>(a->dp, a->desc, lc);
-      adjb_loss_grad_kernel<<<dim3(wblocks, 1), 256, 0, a->stream>>>(a->desc, int(n - 1), slot, lc ^ 1, 0, nx,
-                                                                      a->stride);
-      lc ^= 1;
-    }
-    FVA_CUDA(cudaGetLastError());
+      for (long long n = seg1; n > seg0; --n) {
+        // reverse of step n, whose input is u_{n-1} (segment slot n-1-seg0;
+        // its recorded boundary-applied, y-swept and x-swept states are the
+        // slot's stage grids)
+        const int slot = int(n - 1 - seg0);
+        // diffusion (on S2) and x sweep (on S1): lam[lc] -> tmp1 (adjoint of S1)
+        adjb_sweep_x_kernel<<<dim3(a->sweep_x_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot, lc,
+                                                                               a->stride);
+        // y sweep on B: tmp1 -> tmp0 (adjoint of B)
+        adjb_sweep_y_kernel<<<dim3(a->sweep_y_blocks, 1), 128, 0, a->stream>>>(a->dp, a->desc, int(n), slot,
+                                                                               a->sweep_y_seg, a->stride);
+        // the weights' gradient (side branch) beside the boundary with the
+        // loss gradient of u_{n-1}: lam[lc ^ 1] = lam_{n-1}; both read tmp0,
+        // which the next y sweep overwrites after the join
+        FVA_CUDA(a->fork.fork(a->stream));
+        adjb_weights_kernel<<<dim3((nelem + 3) / 4, 1), 128, 0, a->fork.side>>>(a->dp, a->desc, int(n));
+        adjb_boundary_kernel<<<dim3(grd.x, grd.y, 1), blk, 0, a->stream>>>(a->dp, a->desc, int(n), slot, lc,
+                                                                            a->stride);
+        FVA_CUDA(a->fork.join(a->stream));
+        lc ^= 1;
+      }
+      FVA_CUDA(cudaGetLastError());
+      return FV_OK;
+    });
+    if (rs != FV_OK) return rs;
   }
   FVA_CUDA(cudaStreamSynchronize(a->stream));
   {
@@ -1154,6 +1303,9 @@ struct fv_adjoint_batch {
   size_t ncell = 0, stride = 0;
   int exact = 1;
   cudaStream_t stream = nullptr, own_stream = nullptr;
+  cudaGraphExec_t seg_graph = nullptr;  // the backward's segment graph
+  cudaGraphExec_t rec_graph = nullptr;  // the recorded forward's attempts
+  Fork fork;                            // the weights' branch of a reverse step
   std::vector<fv_loss_window> win;
   std::vector<float *> mem;     // per design: all grids
   std::vector<AdjDesign> hdesc;
@@ -1301,6 +1453,7 @@ fv_status fv_adjoint_batch_create(const fv_params *p, int32_t ndesigns, const fv
     a.nj = w.nj;
     a.first = w.step_first;
     a.last = w.step_last;
+    a.loss_coef = loss_coef(w);
 
     BatchInst &I = b->hinst[d];
     std::memset(&I, 0, sizeof(I));
@@ -1394,6 +1547,9 @@ fv_status fv_adjoint_batch_destroy(fv_adjoint_batch *b) {
   if (b->neg) cudaFree(b->neg);
   if (b->fix) cudaFree(b->fix);
   if (b->frame) cudaFree(b->frame);
+  if (b->seg_graph) cudaGraphExecDestroy(b->seg_graph);
+  if (b->rec_graph) cudaGraphExecDestroy(b->rec_graph);
+  b->fork.release();
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
   return FV_OK;
@@ -1431,15 +1587,18 @@ fv_status fv_adjoint_batch_forward(fv_adjoint_batch *b, const float *amp, const 
   const int rx = std::max(1, b->sms * 4 / nd);
   std::vector<Ctrl> hc(nd);
   long long todo = b->nsteps, attempt = 0;
+  auto one = [&](long long k) -> fv_status {
+    const int rc = launch_b(b, false);
+    if (rc != 0) return afail(FV_CUDA_ERROR, "batch step launch: %s", cudaGetErrorString((cudaError_t)rc));
+    for (size_t g = 0; g < b->sets.size(); ++g)
+      adjb_record_kernel<<<dim3(rx, group_size(b, g)), 256, 0, b->stream>>>(b->sets[g], int(k & 1), int(b->nsteps),
+                                                                           b->stride, b->ncell, b->every, P.nx);
+    return FV_OK;
+  };
   for (int round = 0; round < 64 && todo > 0; ++round) {
-    for (long long k = 0; k < todo; ++k, ++attempt) {
-      const int rc = launch_b(b, false);
-      if (rc != 0) return afail(FV_CUDA_ERROR, "batch step launch: %s", cudaGetErrorString((cudaError_t)rc));
-      for (size_t g = 0; g < b->sets.size(); ++g)
-        adjb_record_kernel<<<dim3(rx, group_size(b, g)), 256, 0, b->stream>>>(b->sets[g], int(attempt & 1),
-                                                                             int(b->nsteps), b->stride, b->ncell,
-                                                                             b->every, P.nx);
-    }
+    const fv_status rs = run_attempts(b->stream, b->rec_graph, attempt, todo, one);
+    if (rs != FV_OK) return rs;
+    attempt += todo;
     FVA_CUDA(cudaGetLastError());
     FVA_CUDA(cudaMemcpyAsync(hc.data(), b->ctrl, sizeof(Ctrl) * nd, cudaMemcpyDeviceToHost, b->stream));
     FVA_CUDA(cudaStreamSynchronize(b->stream));
@@ -1469,6 +1628,7 @@ fv_status fv_adjoint_batch_forward(fv_adjoint_batch *b, const float *amp, const 
 fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, double *grad_phase) {
   if (!b || !grad_amp || !grad_phase) return afail(FV_BAD_ARG, "NULL argument");
   if (!b->have_forward) return afail(FV_BAD_ARG, "no forward run (fv_adjoint_batch_forward) to differentiate");
+  FVA_CUDA(b->fork.init());
   const fv_params &P = b->params;
   const int nx = P.nx, ny = P.ny, nelem = P.array_elems, nd = b->nd;
   const size_t bytes = 3 * b->stride * sizeof(float);
@@ -1477,6 +1637,7 @@ fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, doubl
   for (int d = 0; d < nd; ++d) wmax = std::max(wmax, b->win[d].ni * b->win[d].nj);
   const int lx = (wmax + 255) / 256;
   const dim3 bblk(kBX, kBY);
+  const int bgx = (nx + kBX - 1) / kBX, bgy = (ny + kBY - 1) / kBY;
   for (int d = 0; d < nd; ++d) {
     const AdjDesign &a = b->hdesc[d];
     FVA_CUDA(cudaMemsetAsync(a.acc + 1, 0, 2 * size_t(nelem) * sizeof(double), b->stream));
@@ -1496,34 +1657,38 @@ fv_status fv_adjoint_batch_backward(fv_adjoint_batch *b, double *grad_amp, doubl
   const long long C = b->every;
   for (long long seg0 = ((b->nsteps - 1) / C) * C; seg0 >= 0; seg0 -= C) {
     const long long seg1 = std::min(seg0 + C, b->nsteps);  // steps seg0+1 .. seg1
-    for (int d = 0; d < nd; ++d) {
-      const AdjDesign &a = b->hdesc[d];
-      FVA_CUDA(cudaMemcpyAsync(a.seg, a.ckpt + size_t(seg0 / C) * 3 * b->stride, bytes, cudaMemcpyDeviceToDevice,
-                               b->stream));
-    }
-    for (long long n = seg0 + 1; n <= seg1; ++n) {
-      adjb_sched_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd, int(n - 1), int(n - 1 - seg0), b->stride,
-                                                  b->fix, b->neg, b->cfl_bits);
-      const int rc = launch_b(b, true);
-      if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
-    }
-    for (long long n = seg1; n > seg0; --n) {
-      const int slot = int(n - 1 - seg0);
-      for (size_t g = 0; g < b->sets.size(); ++g) {
-        const AdjDesignSet &S = b->sets[g];
-        const int gn = group_size(b, g);
-        adjb_sweep_x_kernel<<<dim3(b->sweep_x_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot, lc,
-                                                                                b->stride);
-        adjb_sweep_y_kernel<<<dim3(b->sweep_y_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot,
-                                                                                b->sweep_y_seg, b->stride);
-        adjb_weights_kernel<<<dim3((nelem + 3) / 4, gn), 128, 0, b->stream>>>(b->dp, S, int(n));
-        adjb_boundary_kernel<<<dim3((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY, gn), bblk, 0, b->stream>>>(b->dp, S,
-                                                                                                       lc);
-        adjb_loss_grad_kernel<<<dim3(lx, gn), 256, 0, b->stream>>>(S, int(n - 1), slot, lc ^ 1, 0, nx, b->stride);
+    const fv_status rs = run_captured(b->stream, b->seg_graph, [&]() -> fv_status {
+      for (int d = 0; d < nd; ++d) {
+        const AdjDesign &a = b->hdesc[d];
+        FVA_CUDA(cudaMemcpyAsync(a.seg, a.ckpt + size_t(seg0 / C) * 3 * b->stride, bytes, cudaMemcpyDeviceToDevice,
+                                 b->stream));
       }
-      lc ^= 1;
-    }
-    FVA_CUDA(cudaGetLastError());
+      for (long long n = seg0 + 1; n <= seg1; ++n) {
+        adjb_sched_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd, int(n - 1), int(n - 1 - seg0), b->stride,
+                                                    b->fix, b->neg, b->cfl_bits);
+        const int rc = launch_b(b, true);
+        if (rc != 0) return afail(FV_CUDA_ERROR, "replay launch: %s", cudaGetErrorString((cudaError_t)rc));
+      }
+      for (long long n = seg1; n > seg0; --n) {
+        const int slot = int(n - 1 - seg0);
+        for (size_t g = 0; g < b->sets.size(); ++g) {
+          const AdjDesignSet &S = b->sets[g];
+          const int gn = group_size(b, g);
+          adjb_sweep_x_kernel<<<dim3(b->sweep_x_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot, lc,
+                                                                                  b->stride);
+          adjb_sweep_y_kernel<<<dim3(b->sweep_y_blocks, gn), 128, 0, b->stream>>>(b->dp, S, int(n), slot,
+                                                                                  b->sweep_y_seg, b->stride);
+          FVA_CUDA(b->fork.fork(b->stream));
+          adjb_weights_kernel<<<dim3((nelem + 3) / 4, gn), 128, 0, b->fork.side>>>(b->dp, S, int(n));
+          adjb_boundary_kernel<<<dim3(bgx, bgy, gn), bblk, 0, b->stream>>>(b->dp, S, int(n), slot, lc, b->stride);
+          FVA_CUDA(b->fork.join(b->stream));
+        }
+        lc ^= 1;
+      }
+      FVA_CUDA(cudaGetLastError());
+      return FV_OK;
+    });
+    if (rs != FV_OK) return rs;
   }
   // a negative eigenvalue met by the last replay
   adjb_sched_kernel<<<tg, tb, 0, b->stream>>>(b->ddesc, b->inst, nd, 0, 0, b->stride, b->fix, b->neg, b->cfl_bits);
