@@ -1,0 +1,51 @@
+"""The config-4 gradient fixture pinned against itself, on CPU.
+
+tests/golden/adjoint_config4.json holds, for 16 of the phased array's 256
+weights at config 4 (1024 x 1024, 4000 steps), the oracle's tangent-linear
+gradient along the FP32 and the FP64 trajectories and FP64 central
+differences (h = 1e-4 relative) of the loss on the same frozen dt schedule
+(gen_adjoint_config4.py). The FP64 tangent-linear model and the central
+differences are independent routes to the same derivative: their per-
+component agreement pins the oracle's tangent-linear model (the dual-number
+restatement of the step), which the GPU adjoint is then held to
+(test_gpu_adjoint_config4.py).
+"""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _fixture():
+    with open(os.path.join(HERE, "golden", "adjoint_config4.json")) as f:
+        return json.load(f)
+
+
+def test_fp64_tangent_linear_model_agrees_with_fp64_central_differences():
+    fx = _fixture()
+    tlm64, fd64 = np.asarray(fx["tlm64"]), np.asarray(fx["fd64"])
+    assert len(tlm64) == len(fd64) == 16 and np.all(np.isfinite(fd64))
+    rel = np.abs(tlm64 - fd64) / np.abs(fd64)
+    assert rel.max() <= 1e-4, rel  # measured 2.5e-5: the O(h^2) error of the differences
+
+
+def test_fp32_and_fp64_gradients_differ_by_the_fp32_trajectory_error():
+    """Along the FP32 trajectory the gradient moves by about the FP32 state
+    error (~1e-4 relative): well below the adjoint's 1e-3 bar, well above
+    rounding of the derivative arithmetic itself (done in double)."""
+    fx = _fixture()
+    tlm32, tlm64 = np.asarray(fx["tlm32"]), np.asarray(fx["tlm64"])
+    rel = np.abs(tlm32 - tlm64) / np.abs(tlm64)
+    assert 1e-7 < rel.max() <= 1e-3, rel
+    assert abs(fx["loss32"] - fx["loss64"]) <= 1e-3 * fx["loss64"]
+
+
+def test_directions_and_steps():
+    fx = _fixture()
+    case = fx["case"]
+    assert (case["nx"], case["ny"], case["nsteps"], case["elements"]) == (1024, 1024, 4000, 128)
+    assert len(set(fx["directions"])) == 16 and all(0 <= k < 256 for k in fx["directions"])
+    h = np.asarray(fx["fd64_h"])
+    assert np.all(h > 0)
