@@ -230,6 +230,8 @@ PROTOTYPES = {
     "fv_set_division": (C.c_int, [_P, C.c_int32]),
     "fv_get_division": (C.c_int, [_P, _P]),
     "fv_sync": (C.c_int, [_P, C.POINTER(FvRunStats)]),
+    "fv_steps_async": (C.c_int, [_P, C.c_int32]),
+    "fv_step_wait": (C.c_int, [_P, C.POINTER(FvRunStats)]),
     "fv_debug_step": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "fv_set_launch": (C.c_int, [_P, C.c_int32]),
     "fv_set_cta_shape": (C.c_int, [_P, C.c_int32]),

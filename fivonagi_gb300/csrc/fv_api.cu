@@ -10,6 +10,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -18,6 +19,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fv_internal.h"
@@ -57,6 +59,7 @@ __global__ void ctrl_begin_kernel(Ctrl *c, long long remaining, float t_stop) {
   c->accepted = 0;
   c->rejected = 0;
   c->consecutive_rejects = 0;
+  c->mirror_seq = 0;
 }
 
 __global__ void ctrl_reset_kernel(Ctrl *c, float dt, float T, int n) {
@@ -291,6 +294,13 @@ struct fv_handle {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;   // kGraphAttempts attempts
   cudaGraphExec_t graph1 = nullptr;  // fv_run(h, 1): control-block set-up and one attempt
+  // fv_steps_async / fv_step_wait: attempts in flight; each one's finalize
+  // launch writes its control block to the next slot of a host ring
+  HostSlot *ring_host = nullptr, *ring_dev = nullptr;  // kHostRing slots, host and device views
+  cudaGraphExec_t ring_graph = nullptr;   // kGraphAttempts attempts writing the ring
+  cudaGraphExec_t ring_graph1 = nullptr;  // one attempt writing the ring
+  long long ring_enq = 0, ring_got = 0;   // attempts of this run of them enqueued, collected
+  long long ring_acc = 0, ring_rej = 0;   // counters of the last collected attempt
   StepArgs args{};
   int warps = 4;
   bool exact = true;
@@ -481,6 +491,48 @@ void drop_graphs(fv_handle *h) {
   if (h->graph1) cudaGraphExecDestroy(h->graph1);
   h->graph = nullptr;
   h->graph1 = nullptr;
+  if (h->ring_graph) cudaGraphExecDestroy(h->ring_graph);
+  if (h->ring_graph1) cudaGraphExecDestroy(h->ring_graph1);
+  h->ring_graph = nullptr;
+  h->ring_graph1 = nullptr;
+}
+
+// The graphs of attempts whose finalize launches write the host ring: n
+// attempts (kGraphAttempts or 1) into `g`.
+fv_status ensure_ring_graph(fv_handle *h, int n, cudaGraphExec_t &gx) {
+  if (gx) return FV_OK;
+  StepArgs a = h->args;
+  a.host_ring = h->ring_dev;
+  cudaGraph_t g = nullptr;
+  FV_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = 0;
+  for (int k = 0; k < n && rc == 0; ++k) {
+    rc = launch(h, -1, a);
+    if (rc == 0 && h->collect) {
+      collect_kernel<<<1, 1024, 0, h->stream>>>(h->ctrl, h->args.state[0][0], h->args.state[1][0], h->params.nx,
+                                                h->params.ny, h->coll);
+      rc = (int)cudaGetLastError();
+    }
+  }
+  cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+  if (rc != 0) return fail(FV_CUDA_ERROR, "step launch during capture: %s", cudaGetErrorString((cudaError_t)rc));
+  if (ec != cudaSuccess) return fail(FV_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
+  ec = cudaGraphInstantiate(&gx, g, 0);
+  cudaGraphDestroy(g);
+  if (ec != cudaSuccess) {
+    gx = nullptr;
+    return fail(FV_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ec));
+  }
+  return FV_OK;
+}
+
+// Attempts launched by fv_steps_async not yet collected by fv_step_wait:
+// the other runs would reset the counters those attempts report from.
+fv_status check_idle(const fv_handle *h) {
+  if (h->ring_enq != h->ring_got)
+    return fail(FV_BAD_ARG, "%lld attempts in flight: collect them with fv_step_wait first",
+                h->ring_enq - h->ring_got);
+  return FV_OK;
 }
 
 fv_status ensure_graph1(fv_handle *h) {
@@ -801,6 +853,7 @@ fv_status fv_destroy(fv_handle *h) {
   if (h->coll_mem) cudaFree(h->coll_mem);
   if (h->snap_mem) cudaFree(h->snap_mem);
   if (h->snap_ctrl) cudaFree(h->snap_ctrl);
+  if (h->ring_host) cudaFreeHost(h->ring_host);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return FV_OK;
@@ -1048,6 +1101,7 @@ fv_status fv_get_stats(fv_handle *h, fv_run_stats *out) {
 
 fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts) {
   if (!h || nattempts < 0) return fail(FV_BAD_ARG, "bad argument");
+  if (fv_status busy = check_idle(h)) return busy;
   ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nattempts,
                                             std::numeric_limits<float>::infinity());
   FV_CUDA(cudaGetLastError());
@@ -1056,6 +1110,7 @@ fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts) {
 
 fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_ms, float *attempt_ms) {
   if (!h || nattempts < 1 || !step_kernel_ms || !attempt_ms) return fail(FV_BAD_ARG, "bad argument");
+  if (fv_status busy = check_idle(h)) return busy;
   ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, (long long)nattempts,
                                             std::numeric_limits<float>::infinity());
   FV_CUDA(cudaGetLastError());
@@ -1099,6 +1154,7 @@ fv_status fv_time_attempts(fv_handle *h, int32_t nattempts, float *step_kernel_m
 
 fv_status fv_time_run(fv_handle *h, int64_t nattempts, float *ms) {
   if (!h || nattempts < 1 || !ms) return fail(FV_BAD_ARG, "bad argument");
+  if (fv_status busy = check_idle(h)) return busy;
   cudaEvent_t ev[2] = {};
   for (int k = 0; k < 2; ++k) {
     const cudaError_t e = cudaEventCreate(&ev[k]);
@@ -1140,8 +1196,74 @@ fv_status fv_sync(fv_handle *h, fv_run_stats *out) {
   return h->ctrl_host->status ? (fv_status)h->ctrl_host->status : FV_OK;
 }
 
+fv_status fv_steps_async(fv_handle *h, int32_t nattempts) {
+  if (!h || nattempts < 1) return fail(FV_BAD_ARG, "bad argument");
+  if (h->ring_enq - h->ring_got + nattempts > kHostRing)
+    return fail(FV_BAD_ARG, "more than %d attempts in flight: collect some with fv_step_wait", kHostRing);
+  if (!h->ring_host) {
+    FV_CUDA(cudaHostAlloc(&h->ring_host, kHostRing * sizeof(HostSlot), cudaHostAllocMapped));
+    FV_CUDA(cudaHostGetDevicePointer(&h->ring_dev, h->ring_host, 0));
+  }
+  fv_status s = ensure_ring_graph(h, kGraphAttempts, h->ring_graph);
+  if (s == FV_OK) s = ensure_ring_graph(h, 1, h->ring_graph1);
+  if (s != FV_OK) return s;
+  if (h->ring_enq == h->ring_got) {
+    // a new run of enqueued attempts (every earlier one collected, so no
+    // ring write is pending): no step budget or stop time, counters and the
+    // ring's sequence from zero
+    std::memset(h->ring_host, 0, kHostRing * sizeof(HostSlot));
+    h->ring_enq = h->ring_got = 0;
+    h->ring_acc = h->ring_rej = 0;
+    ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, std::numeric_limits<long long>::max(),
+                                              std::numeric_limits<float>::infinity());
+    FV_CUDA(cudaGetLastError());
+  }
+  for (int k = 0; k < nattempts;) {
+    const bool whole = nattempts - k >= kGraphAttempts;
+    FV_CUDA(cudaGraphLaunch(whole ? h->ring_graph : h->ring_graph1, h->stream));
+    k += whole ? kGraphAttempts : 1;
+  }
+  h->ring_enq += nattempts;
+  return FV_OK;
+}
+
+fv_status fv_step_wait(fv_handle *h, fv_run_stats *out) {
+  if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (h->ring_got == h->ring_enq) return fail(FV_BAD_ARG, "no attempt in flight (fv_steps_async)");
+  const long long i = h->ring_got;
+  const HostSlot &slot = h->ring_host[i % kHostRing];
+  const uint32_t pass = uint32_t(i / kHostRing) + 1u;
+  const volatile uint32_t *gen = &slot.gen;
+  // the device writes the block, then the pass; a wait that outlives the
+  // stream's work (an error, or the attempts done without the write) ends
+  for (unsigned spin = 1; *gen != pass; ++spin) {
+    if ((spin & 1023u) == 0u) {
+      const cudaError_t e = cudaStreamQuery(h->stream);
+      if (e == cudaSuccess && *gen != pass) return fail(FV_CUDA_ERROR, "attempt done without its control block");
+      if (e != cudaSuccess && e != cudaErrorNotReady) return fail(FV_CUDA_ERROR, "%s", cudaGetErrorString(e));
+      std::this_thread::yield();
+    }
+  }
+  std::atomic_thread_fence(std::memory_order_acquire);
+  ++h->ring_got;
+  std::memcpy(h->ctrl_host, (const void *)&slot.c, sizeof(Ctrl));
+  fill_stats(h, out);
+  const Ctrl &c = *h->ctrl_host;
+  if (out) {
+    out->accepted = c.accepted - h->ring_acc;
+    out->rejected = c.rejected - h->ring_rej;
+  }
+  h->ring_acc = c.accepted;
+  h->ring_rej = c.rejected;
+  const int st = c.status;
+  if (st == FV_NEGATIVE_EIGENVALUE) return fail(FV_NEGATIVE_EIGENVALUE, "negative eigenvalue (tmp3 < 0)");
+  if (st == FV_DT_TOO_LARGE) return fail(FV_DT_TOO_LARGE, "dt too large after %d retries", h->dp.max_retries);
+  return st ? (fv_status)st : FV_OK;
+}
+
 fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
   if (!h || nsteps < 0) return fail(FV_BAD_ARG, "bad argument");
+  if (fv_status busy = check_idle(h)) return busy;
   long long todo = nsteps;
   bool have_ctrl = false;  // ctrl_host holds the control block after the launches
   if (nsteps == 1) {
@@ -1178,6 +1300,7 @@ fv_status fv_run(fv_handle *h, int64_t nsteps, fv_run_stats *out) {
 
 fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out) {
   if (!h) return fail(FV_BAD_ARG, "handle is NULL");
+  if (fv_status busy = check_idle(h)) return busy;
   ctrl_begin_kernel<<<1, 1, 0, h->stream>>>(h->ctrl, std::numeric_limits<long long>::max(),
                                             float(t_stop));
   FV_CUDA(cudaGetLastError());
@@ -1249,6 +1372,7 @@ fv_status fv_get_division(fv_handle *h, int32_t *mode) {
 
 fv_status fv_debug_step(fv_handle *h, int32_t stage, float *u1, float *u2, float *u3) {
   if (!h || !u1 || !u2 || !u3) return fail(FV_BAD_ARG, "NULL argument");
+  if (fv_status busy = check_idle(h)) return busy;
   if (stage < FV_STAGE_BOUNDARY || stage > FV_STAGE_SOURCE) return fail(FV_BAD_ARG, "bad stage %d", stage);
   if (!h->dbg_mem) FV_CUDA(cudaMalloc(&h->dbg_mem, 3 * h->field_stride * sizeof(float)));
   StepArgs a = h->args;

@@ -107,7 +107,19 @@ struct Ctrl {
   int64_t rejected;
   uint32_t blocks_done;   // unused (zero)
   int32_t last_accepted;  // the last decided attempt was accepted (1) or rejected (0)
+  int64_t mirror_seq;     // attempts whose control block went to the host ring
 };
+
+// One slot of the host ring that finalize_kernel writes when StepArgs'
+// host_ring is set: the attempt's control block, then its pass over the
+// ring (the host waits until `gen` reaches the pass it expects).
+constexpr int kHostRing = 64;
+struct HostSlot {
+  Ctrl c;
+  uint32_t gen;
+  uint32_t pad;
+};
+static_assert(sizeof(Ctrl) % 4 == 0, "the finalize launch copies the control block in words");
 
 // Ghost frame: the boundary hook's values of the ghost cells (the two
 // outermost rows and columns), written by a small pre-pass each attempt and
@@ -178,6 +190,9 @@ struct StepArgs {
   int32_t div_exact;      // attempts (-1, kLaunchStep) run the step kernel with exact
                           // division (kStageExactDiv) instead of FMA division
   int32_t shape;          // CTA shape of the exact-division step kernel (kStepShapes)
+  HostSlot *host_ring;    // or nullptr: the finalize launch also copies the control
+                          // block, decided or not, to slot mirror_seq % kHostRing
+                          // of this ring (mapped pinned host memory)
 };
 
 // CTA shapes of the exact-division step kernel: {warps per CTA, CTAs per

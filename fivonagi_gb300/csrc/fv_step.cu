@@ -757,8 +757,22 @@ constexpr int kFinalizeThreads = 1024;  // one CTA; enough threads that the part
 
 __global__ void __launch_bounds__(kFinalizeThreads) finalize_kernel(StepArgs a) {
   __shared__ float red[kFinalizeThreads / 32];
-  if (!attempt_active(a.ctrl)) return;
-  finalize(a, red);
+  if (attempt_active(a.ctrl)) finalize(a, red);
+  if (a.host_ring && threadIdx.x == 0) {
+    // the attempt's control block for the host, without a copy launch
+    // (finalize's own writes came from this thread): the block, then the
+    // slot's pass number, which the host polls
+    volatile Ctrl *vc = a.ctrl;
+    const long long q = vc->mirror_seq;
+    vc->mirror_seq = q + 1;
+    HostSlot *slot = a.host_ring + (q % kHostRing);
+    const volatile uint32_t *src = reinterpret_cast<const volatile uint32_t *>(a.ctrl);
+    volatile uint32_t *dst = reinterpret_cast<volatile uint32_t *>(&slot->c);
+    for (int w = 0; w < int(sizeof(Ctrl) / 4); ++w) dst[w] = src[w];
+    __threadfence_system();
+    *reinterpret_cast<volatile uint32_t *>(&slot->gen) = uint32_t(q / kHostRing) + 1u;
+    __threadfence_system();
+  }
 }
 
 // The app's boundary hook (boundary(), apps/*/boundary.h) evaluated for

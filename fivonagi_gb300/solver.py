@@ -202,6 +202,33 @@ class Simulation:
         check(self.lib.fv_sync(self.h, C.byref(st)), "fv_sync")
         return st.as_dict()
 
+    def steps_async(self, n: int) -> None:
+        """Enqueue n attempts without synchronising (fv_steps_async; at most
+        64 in flight)."""
+        check(self.lib.fv_steps_async(self.h, int(n)), "fv_steps_async")
+
+    def step_wait(self) -> dict:
+        """Stats of the oldest attempt in flight, once it has completed
+        (fv_step_wait)."""
+        st = FvRunStats()
+        check(self.lib.fv_step_wait(self.h, C.byref(st)), "fv_step_wait")
+        return st.as_dict()
+
+    def steps_pipelined(self, n: int, block: int = 32):
+        """n attempts with every attempt's stats read back, the next block of
+        attempts enqueued before the current block is read; yields each
+        attempt's stats in order."""
+        block = max(1, min(block, 32))
+        queued = min(n, block)
+        if queued:
+            self.steps_async(queued)
+        for k in range(n):
+            if k % block == 0 and queued < n:
+                m = min(block, n - queued)
+                self.steps_async(m)
+                queued += m
+            yield self.step_wait()
+
     def set_launch(self, blocks: int) -> None:
         """CTAs per step launch (0 = default); see fv_set_launch."""
         check(self.lib.fv_set_launch(self.h, int(blocks)), "fv_set_launch")

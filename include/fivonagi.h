@@ -275,6 +275,30 @@ fv_status fv_run_until(fv_handle *h, double t_stop, fv_run_stats *out);
 fv_status fv_launch_attempts(fv_handle *h, int64_t nattempts);
 fv_status fv_sync(fv_handle *h, fv_run_stats *out);
 
+/* Step attempts with every attempt's stats read back, pipelined: the
+ * per-step host read of the calcFrame loop (common/main.cu:310-635 copies T
+ * and n to the host every step) without stopping the GPU for it.
+ * fv_steps_async enqueues nattempts attempts (in the same captured graphs
+ * as fv_run) and returns without synchronising; at most 64 attempts may be
+ * in flight (FV_BAD_ARG beyond). Each attempt's last launch writes its
+ * control block to a slot of mapped pinned host memory. fv_step_wait waits
+ * for the oldest attempt in flight and returns its stats (accepted 1 or 0,
+ * rejected 0 or 1, dt, T, CFL, n) and status, as fv_run does. A run of
+ * enqueued attempts has no step budget or stop time; consecutive
+ * rejections carry over between its attempts, so max_retries ends a run of
+ * rejections with FV_DT_TOO_LARGE, and an attempt enqueued after a failed
+ * one does nothing and reports the same status. While attempts are in
+ * flight, fv_run, fv_run_until, fv_launch_attempts, fv_time_* and
+ * fv_debug_step return FV_BAD_ARG. A caller keeps a block of attempts
+ * queued ahead of the one it reads (n a multiple of 32 here):
+ *   fv_steps_async(h, 32);
+ *   for (k = 0; k < n; ++k) {
+ *     if (k % 32 == 0 && k + 32 < n) fv_steps_async(h, 32);
+ *     fv_step_wait(h, &st);
+ *   } */
+fv_status fv_steps_async(fv_handle *h, int32_t nattempts);
+fv_status fv_step_wait(fv_handle *h, fv_run_stats *out);
+
 /* Runs nattempts attempts one at a time, without graph capture, with CUDA
  * events on the handle's stream between the attempt's launches, and returns
  * the step kernel's average duration and the whole attempt's, in ms.

@@ -378,6 +378,56 @@ def test_single_step_runs_match_a_multi_step_run_and_retry_rejections():
     many.close()
 
 
+def test_pipelined_attempts_match_the_oracle_and_the_synchronous_path():
+    """fv_steps_async / fv_step_wait: attempts enqueued a block ahead of the
+    one whose stats are read. Each attempt's stats (accepted or rejected, dt, T)
+    equal those of the same attempt launched and read synchronously
+    (fv_launch_attempts(1) + fv_sync), a rejected first attempt included,
+    and the final state is the oracle's after the same accepted steps and
+    rejections."""
+    p = small_params(2, 64, 32).replace(dtini=0.3)  # the first attempt is rejected
+    orc = OracleSim(p, np.float32, math="fvm")
+    orc.init_state()
+    u = orc.get_state()
+    sim = Simulation(p)
+    sim.set_state(*u)
+    got = list(sim.steps_pipelined(12, block=4))
+    assert got[0]["accepted"] == 0 and got[0]["rejected"] == 1
+    assert all(st["accepted"] + st["rejected"] == 1 and st["status"] == 0 for st in got)
+    last = max(k for k, st in enumerate(got) if st["accepted"])
+    accepted = sum(st["accepted"] for st in got)
+    so = orc.run(accepted)
+    assert so["rejected"] == sum(st["rejected"] for st in got[: last + 1])
+    a, o = sim.get_state(), orc.get_state()
+    for f in range(3):
+        assert same_values(a[f], o[f])
+    ref = Simulation(p)
+    ref.set_state(*u)
+    for st in got:
+        ref.launch_attempts(1)
+        sr = ref.sync()
+        assert np.float32(st["T"]) == np.float32(sr["T"]) and np.float32(st["dt"]) == np.float32(sr["dt"])
+        assert st["n"] == sr["n"]
+    # 64 attempts in flight at most (the ring passes over its slots more
+    # than once here), no other run while any is, and nothing to wait for
+    # when none is
+    sim.steps_async(40)
+    for _ in range(30):
+        st = sim.step_wait()
+        assert st["accepted"] + st["rejected"] == 1
+    sim.steps_async(54)
+    with pytest.raises(_abi.FvError):
+        sim.steps_async(1)
+    with pytest.raises(_abi.FvError):
+        sim.run(1)
+    T = [sim.step_wait()["T"] for _ in range(64)]
+    assert all(b >= a for a, b in zip(T, T[1:])) and T[-1] > T[0]
+    with pytest.raises(_abi.FvError):
+        sim.step_wait()
+    assert sim.run(1)["accepted"] == 1
+    sim.close()
+    ref.close()
+
 
 @pytest.mark.parametrize("app", [0, 2])
 @pytest.mark.parametrize("division", [_abi.FV_DIVISION_EXACT, _abi.FV_DIVISION_FMA])
