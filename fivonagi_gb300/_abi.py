@@ -44,7 +44,7 @@ FV_APP_FOCUSED_BEAM = 3
 FV_APP_PHASED_ARRAY = 4
 
 # CTA shapes of the step kernel (fv_set_cta_shape): warps per CTA x CTAs per SM
-FV_CTA_SHAPES = {0: "4x4", 1: "2x8", 2: "1x16", 3: "1x18"}
+FV_CTA_SHAPES = {0: "4x4", 1: "2x8", 2: "1x16", 3: "1x18", 4: "4x4/ahead1", 5: "4x4/ahead3"}
 
 # division in the step kernel (fv_set_division)
 FV_DIVISION_DEFAULT = -1

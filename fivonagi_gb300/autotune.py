@@ -5,7 +5,8 @@ results (every warp streams its own share of the grid's (window, row) work
 with the same arithmetic):
   * the CTA shape (fv_set_cta_shape): warps per CTA and the CTAs per SM the
     kernel is built for -- 4 x 4, 2 x 8, 1 x 16, or 1 x 18 with a smaller
-    register budget and more warps per SM;
+    register budget and more warps per SM -- and the sweep's prefetch depth,
+    the input rows loaded ahead of the row in use (2, or 1 and 3 at 4 x 4);
   * the number of persistent CTAs (fv_set_launch), in waves of the CTAs
     resident at once: more waves keep every SM full to the end but repeat
     the streaming loop's warm-up rows on shorter segments;
@@ -26,7 +27,7 @@ from . import _abi
 from ._abi import FvParams
 
 CACHE = os.path.join(_abi.LIB_DIR, "autotune.json")
-CACHE_VERSION = 2
+CACHE_VERSION = 3
 WAVES = (1, 2, 3, 4, 6, 8)
 SHAPES = tuple(_abi.FV_CTA_SHAPES)
 

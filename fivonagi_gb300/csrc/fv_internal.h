@@ -196,10 +196,11 @@ struct StepArgs {
 };
 
 // CTA shapes of the exact-division step kernel: {warps per CTA, CTAs per
-// SM it is built for}. 0: 4 x 4 (16 warps per SM), 1: 2 x 8, 2: 1 x 16,
-// 3: 1 x 18 (18 warps per SM, at most 112 registers a thread). The
-// FMA-division and stage-recording kernels run shape 0.
-constexpr int kStepShapes = 4;
+// SM it is built for, rows loaded ahead}. 0: 4 x 4 (16 warps per SM), 1:
+// 2 x 8, 2: 1 x 16, 3: 1 x 18 (18 warps per SM, at most 112 registers a
+// thread), all loading 2 rows ahead; 4 and 5: 4 x 4 loading 1 and 3 rows
+// ahead. The FMA-division and stage-recording kernels run shape 0.
+constexpr int kStepShapes = 6;
 
 // One simulation of a batch: its parameters, buffers and control block,
 // and where its window-rows start in the batch's concatenated work.

@@ -585,7 +585,7 @@ __device__ __forceinline__ void publish(const StepArgs &a, float cmax, bool neg,
 // budget): the CTA shape (StepArgs::shape) only changes how the launch's
 // warps are grouped and how many fit on an SM; every warp streams its own
 // share either way.
-template <int STAGE, int W>
+template <int STAGE, int W, int PRE = 2>
 __device__ __forceinline__ void step_body(const StepArgs &a) {
   __shared__ float red[W];
   __shared__ int sh[1];
@@ -635,10 +635,10 @@ __device__ __forceinline__ void step_body(const StepArgs &a) {
     const int xw = win * kWarpCols;
     if constexpr (STAGE < 0) {
       StepMarker mk{a, -1};
-      stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+      stream_window<STAGE, DP, PRE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
     } else {
       NoMarker mk;
-      stream_window<STAGE, DP>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
+      stream_window<STAGE, DP, PRE>(a.p, in, frame, out, xw, y0, y1, dt, T, mdx, mdy, shx, shy, cmax, neg, mk);
     }
     pos += y1 - y0;
   }
@@ -646,9 +646,11 @@ __device__ __forceinline__ void step_body(const StepArgs &a) {
   publish<W>(a, cmax, neg, blockIdx.x, red, sh);
 }
 
-template <int STAGE, int W = kWarps, int MINB = 4>
+// PRE: input rows loaded ahead of the row in use (2 by default; the
+// autotuner also times 1 and 3 in shapes 4 and 5).
+template <int STAGE, int W = kWarps, int MINB = 4, int PRE = 2>
 __global__ void __launch_bounds__(W * kLanes, MINB) step_kernel(StepArgs a) {
-  step_body<STAGE, W>(a);
+  step_body<STAGE, W, PRE>(a);
 }
 
 // One-warp CTAs with a register cap (__maxnreg__ cannot join
@@ -666,6 +668,8 @@ static void *exact_step_ptr(int shape, int &threads) {
     case 1: threads = 2 * kLanes; return (void *)step_kernel<kStageExactDiv, 2, 8>;
     case 2: threads = kLanes; return (void *)step_kernel_r<kStageExactDiv, 128>;
     case 3: threads = kLanes; return (void *)step_kernel_r<kStageExactDiv, 112>;
+    case 4: threads = kThreads; return (void *)step_kernel<kStageExactDiv, kWarps, 4, 1>;
+    case 5: threads = kThreads; return (void *)step_kernel<kStageExactDiv, kWarps, 4, 3>;
     default: threads = kThreads; return (void *)step_kernel<kStageExactDiv, kWarps, 4>;
   }
 }
@@ -675,6 +679,8 @@ static void launch_exact_step(const StepArgs &a, cudaStream_t st) {
     case 1: step_kernel<kStageExactDiv, 2, 8><<<a.nblocks, 2 * kLanes, 0, st>>>(a); break;
     case 2: step_kernel_r<kStageExactDiv, 128><<<a.nblocks, kLanes, 0, st>>>(a); break;
     case 3: step_kernel_r<kStageExactDiv, 112><<<a.nblocks, kLanes, 0, st>>>(a); break;
+    case 4: step_kernel<kStageExactDiv, kWarps, 4, 1><<<a.nblocks, kThreads, 0, st>>>(a); break;
+    case 5: step_kernel<kStageExactDiv, kWarps, 4, 3><<<a.nblocks, kThreads, 0, st>>>(a); break;
     default: step_kernel<kStageExactDiv><<<a.nblocks, kThreads, 0, st>>>(a); break;
   }
 }

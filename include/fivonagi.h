@@ -329,7 +329,9 @@ fv_status fv_get_launch(fv_handle *h, int32_t *blocks, int32_t *max_resident);
 
 /* CTA shape of the step kernel, for the autotuner: 0 = 4 warps per CTA,
  * 4 CTAs per SM (the default); 1 = 2 warps, 8 per SM; 2 = 1 warp, 16 per
- * SM; 3 = 1 warp, 18 per SM (built for at most 112 registers a thread).
+ * SM; 3 = 1 warp, 18 per SM (built for at most 112 registers a thread);
+ * all loading input rows 2 ahead of the row in use; 4 and 5 = shape 0
+ * loading 1 and 3 rows ahead (the sweep's prefetch depth).
  * Every warp streams its own share of the grid in every shape, so the
  * results are the same bit for bit; what changes is how many warps an SM
  * holds and how the launch groups them. Applies to the exact-division

@@ -485,11 +485,12 @@ def test_few_ctas_match_oracle(app, nx, ny, blocks):
     sim.close()
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3])
+@pytest.mark.parametrize("shape", sorted(_abi.FV_CTA_SHAPES))
 @pytest.mark.parametrize("app,nx,ny", [(3, 300, 130), (1, 64, 64), (0, 100, 37)])
 def test_cta_shapes_match_oracle(shape, app, nx, ny):
-    """Every CTA shape of the step kernel (warps per CTA x CTAs per SM),
-    at its default CTA count and at a few CTAs, gives the oracle's result."""
+    """Every CTA shape of the step kernel (warps per CTA x CTAs per SM x
+    rows loaded ahead), at its default CTA count and at a few CTAs, gives
+    the oracle's result."""
     p = small_params(app, nx, ny)
     orc = OracleSim(p, np.float32, math="fvm")
     orc.init_state()
