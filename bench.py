@@ -611,9 +611,12 @@ def run_gpu(args):
         "frac": achieved / peak,
         "peak_source": f"hbm_gbs, {peak_kind} (MEASURED_PEAKS.json); of measured",
         "traffic": prof.get("bytes_per_launch"),
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch "
-                          "(profiles/step_kernel_focused_beam_4096x2048.md)",
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch in CTA "
+                          "shape 4x4 (profiles/step_kernel_focused_beam_4096x2048.md)",
         "kernel": "step_kernel (fused y/x sweeps, CFL, diffusion)",
+        "launch": {"cta_shape": _abi.FV_CTA_SHAPES.get(launch.shape, str(launch.shape)), "ctas": launch.blocks,
+                   "division": {_abi.FV_DIVISION_EXACT: "exact", _abi.FV_DIVISION_FMA: "fma"}.get(
+                       launch.division, "library default (exact)")},
         "bytes_per_launch": alg_bytes,
         "launch_ms": step_kernel_ms,
         "launch_timing": "step kernel alone, CUDA events between an attempt's launches on the solver's stream",
@@ -982,7 +985,7 @@ def main():
                          "case for a profiler's launch list)")
     ap.add_argument("--blocks", type=int, default=0,
                     help="plain workload: CTAs per step launch instead of the autotuner's choice")
-    ap.add_argument("--shape", type=int, default=-1, choices=[-1, *range(4)],
+    ap.add_argument("--shape", type=int, default=-1, choices=[-1, *range(6)],
                     help="plain workload: the step kernel's CTA shape (fv_set_cta_shape) instead of the "
                          "autotuner's (or, with --blocks, shape 0)")
     ap.add_argument("--division", choices=["default", "fma", "exact"], default="default",

@@ -27,8 +27,9 @@ from . import _abi
 from ._abi import FvParams
 
 CACHE = os.path.join(_abi.LIB_DIR, "autotune.json")
-CACHE_VERSION = 3
+CACHE_VERSION = 4
 WAVES = (1, 2, 3, 4, 6, 8)
+MARGIN = 0.01  # another shape or division replaces the default only if this much faster
 SHAPES = tuple(_abi.FV_CTA_SHAPES)
 
 
@@ -94,6 +95,14 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> Launch:
                 results[Launch(w * resident, mode, shape)] = sim.time_run(steps) / steps
                 sim.sync()
         best = min(results, key=results.get)
+        # keep the default shape (profiled, and the one the other kernels
+        # share) unless another is clearly faster: near-ties are noise and
+        # depend on the state the candidates were timed on
+        default = [c for c in results if c.shape == 0 and c.division == _abi.FV_DIVISION_EXACT]
+        if default:
+            d = min(default, key=results.get)
+            if results[best] > (1.0 - MARGIN) * results[d]:
+                best = d
     finally:
         sim.close()
     cache[key] = {"blocks": best.blocks, "division": best.division, "shape": best.shape,
