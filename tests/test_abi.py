@@ -94,7 +94,9 @@ def test_bad_arguments_are_rejected_before_any_device_work():
     lib = _abi.load_library()
     h = C.c_void_p()
     p = _abi.default_params("plane-wave")
-    for bad in (p.replace(nx=4), p.replace(app=9), p.replace(xmax=-1.0), p.replace(dtini=0.0),
+    for bad in (p.replace(nx=4), p.replace(ny=7), p.replace(nx=65536, ny=32768),  # below 8x8, above 2^30 cells
+                p.replace(app=9), p.replace(xmax=-1.0), p.replace(dtini=0.0),
+                p.replace(cflmax=0.0), p.replace(cflwhish=-1.0),
                 _abi.default_params("focused-beam").replace(ramp_periods=0.0),
                 _abi.default_params("phased-array").replace(array_elems=0),
                 _abi.default_params("phased-array").replace(array_elems=100)):
@@ -104,6 +106,8 @@ def test_bad_arguments_are_rejected_before_any_device_work():
     assert lib.fv_default_params(42, C.byref(p)) == _abi.FV_BAD_ARG
     assert lib.fv_destroy(None) == _abi.FV_OK
     assert lib.fv_run(None, 1, None) == _abi.FV_BAD_ARG
+    assert lib.fv_steps_async(None, 1) == _abi.FV_BAD_ARG
+    assert lib.fv_step_wait(None, None) == _abi.FV_BAD_ARG
 
 
 def test_no_device_is_a_status_not_a_crash():
