@@ -85,3 +85,37 @@ def test_recorder_writes_the_frame_files(tmp_path):
         assert want in names
     assert rec.n_done > 0
     sim.close()
+
+
+def test_pipelined_attempts_collect_like_a_run():
+    """The pipelined calls (fv_steps_async / fv_step_wait) run the attempts
+    in graphs of their own, with the collection launch after each one: with
+    the window moving, the state, every attempt's T and the collected
+    series equal those of one fv_run of the same steps."""
+    p = small_params(0, 96, 48).replace(moving_domain=1, mdt=0.5, mdvx=1.0, mdvy=0.0)
+    probes = [(20, 2), (40, 2), (55, 10)]
+    nsteps = 70
+    runs = []
+    for pipelined in (False, True):
+        sim = Simulation(p)
+        sim.init_state()
+        sim.collect_enable(probes=probes, envelope_row=2, envelope_len=4 * p.nx, capacity=256,
+                           envelope_halfwidth=0.5)
+        if pipelined:
+            acc = 0
+            while acc < nsteps:  # as many attempts as steps remain (a rejection needs another round)
+                for st in sim.steps_pipelined(nsteps - acc):
+                    acc += st["accepted"]
+                    T = st["T"]
+            assert acc == nsteps
+        else:
+            T = sim.run(nsteps)["T"]
+        runs.append((sim.get_state(), sim.collect_read(), T, sim.stats()["mdx"]))
+        sim.close()
+    (a, ca, Ta, ma), (b, cb, Tb, mb) = runs
+    assert ma == mb > 0 and np.float32(Ta) == np.float32(Tb)
+    for f in range(3):
+        np.testing.assert_array_equal(a[f], b[f])
+    for key in ("T", "cfl", "probes", "envelope"):
+        np.testing.assert_array_equal(ca[key], cb[key])
+    assert ca["steps"] == cb["steps"] > 0
