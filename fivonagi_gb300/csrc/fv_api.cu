@@ -487,6 +487,8 @@ void fill_stats(const fv_handle *h, fv_run_stats *st) {
 // The captured graphs hold the launch shape, division and collector of
 // when they were captured: changing any of them drops them.
 void drop_graphs(fv_handle *h) {
+  // attempts enqueued by fv_steps_async may still run from these graphs
+  if (h->ring_enq != h->ring_got && h->stream) cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->graph1) cudaGraphExecDestroy(h->graph1);
   h->graph = nullptr;
