@@ -909,6 +909,7 @@ def designs_report(args, batch: int) -> dict:
     same = all(np.array_equal(conc_grads[d][0], grads[d][0]) and np.array_equal(conc_grads[d][1], grads[d][1])
                for d in range(n_conc))
     return {
+        **_designs_fp64_check(grads, nsteps, args.seed),
         "value": args.designs / t_batched, "unit": "gradients/s",
         "designs": args.designs, "designs_per_batch": batch, "steps": nsteps,
         "forward_plain_s": t_plain,
@@ -923,6 +924,29 @@ def designs_report(args, batch: int) -> dict:
         "workload": f"phased array 2048x1024, {nsteps} steps, 128 elements x (amplitude, phase), 32x32 focal "
                     f"windows from an 8x8 grid in the right half, seed {args.seed}",
     }
+
+
+def _designs_fp64_check(grads, nsteps, seed) -> dict:
+    """Design 0's batched gradient against FP64 central differences of its
+    loss on the same dt schedule (the committed fixture made on the host by
+    tests/golden/gen_adjoint_config5.py), on the fixture's weights; only for
+    the fixture's case (6000 steps, seed 0)."""
+    import numpy as np
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "adjoint_config5.json")
+    if nsteps != 6000 or seed != 0 or grads[0] is None or not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        fx = json.load(f)
+    if len(fx.get("fd64", [])) != len(fx.get("directions", [])) or None in fx["fd64"]:
+        return {}
+    g = np.concatenate(grads[0])[np.asarray(fx["directions"])]
+    fd = np.asarray(fx["fd64"])
+    rel = np.abs(g - fd) / np.abs(fd)
+    return {"gradient_error_vs_fp64": {
+        "design": 0, "weights": fx["direction_names"], "rel": [float(x) for x in rel], "max_rel": float(rel.max()),
+        "reference": "FP64 central differences (h = 1e-4 relative) of the design's loss on its dt schedule, "
+                     "computed on the host by the oracle"}}
 
 
 def run_designs(args):

@@ -49,3 +49,17 @@ def test_directions_and_steps():
     assert len(set(fx["directions"])) == 16 and all(0 <= k < 256 for k in fx["directions"])
     h = np.asarray(fx["fd64_h"])
     assert np.all(h > 0)
+
+
+def test_fixture_parameters_are_the_library_defaults():
+    """The generators build the phased array's parameters without the
+    library (the oracle runs on the host); they must be the library's own
+    defaults, with config 5's grid as bench.py's designs workload sets it."""
+    from fivonagi_gb300 import _abi
+    from tests.golden.gen_adjoint_config4 import config4_params
+    from tests.golden.gen_adjoint_config5 import config5_params
+
+    lib = _abi.default_params("phased-array")
+    assert config4_params().as_dict() == lib.as_dict()
+    c5 = lib.replace(nx=2048, ny=1024, xmax=2047 / 24, ymax=1023 / 24, center=512.0)
+    assert config5_params().as_dict() == c5.as_dict()
