@@ -20,8 +20,9 @@ the FP64 solution:
            evaluation, to within 1.5x;
       d(fvm32, libm32) <= 2.5 * d(libm32, fp64) + 1e-7
         -- implied by the first through the triangle inequality.
-  * The benchmark spec's 1e-5 between the two FP32 oracles holds up to the
-    step counts listed per app (N_1e5); beyond them the bar above applies.
+  * A bar of 1e-5 (relative L2 per field) between the two FP32 oracles
+    holds up to the step counts listed per app (N_1e5); beyond them the bar
+    above applies.
     Against the fvm oracle it holds at every N (the distance is 0).
 
 Configurations: 1 = plane wave (no transcendental hook: the two FP32
