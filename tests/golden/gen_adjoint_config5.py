@@ -62,7 +62,7 @@ def config5_case(p, d: int = DESIGN):
     wr = np.random.default_rng(DESIGN_SEED + d)
     amp = (wr.uniform(0.5, 1.5, p.array_elems) * p.ampl).astype(np.float32)
     ph = wr.uniform(0.0, 2 * np.pi, p.array_elems).astype(np.float32)
-    i, j = targets[d]
+    i, j = (int(x) for x in targets[d])
     window = (i - 16, j - 16, 32, 32, max(1, NSTEPS - 499), NSTEPS)
     dirs = np.sort(np.random.default_rng(DIR_SEED).choice(2 * p.array_elems, NDIR, replace=False)).astype(np.int32)
     return amp, ph, window, dirs
