@@ -42,7 +42,7 @@ def test_c_driver_matches_the_python_binding(tmp_path):
     from fivonagi_gb300 import Simulation
 
     exe = _build(tmp_path)
-    nx, ny, nprint, dtprint, npipe = 128, 96, 3, 1.0, 10
+    nx, ny, nprint, dtprint, npipe = 128, 96, 18, 1.0, 10  # past T = 0, where the source starts (TIDE = 15)
     out = tmp_path / "u.bin"
     r = subprocess.run([exe, str(nx), str(ny), str(nprint), str(dtprint), str(npipe), str(out)],
                        capture_output=True, text=True, check=True)
