@@ -887,6 +887,36 @@ def designs_report(args, batch: int) -> dict:
             grads[d] = (ga[k], gp[k])
         ab.close()
     t_batched = t_fwd + t_bwd
+    # optionally: smaller batches, several at once, each on its own stream
+    # from a host thread (their launch sequences overlap as the single
+    # handles' do)
+    conc_batched = None
+    if args.batch_streams > 1:
+        from concurrent.futures import ThreadPoolExecutor as _TPE
+
+        size = max(1, args.stream_batch)
+        groups = [list(range(b0, min(args.designs, b0 + size))) for b0 in range(0, args.designs, size)]
+
+        def run_group(ds):
+            ab = AdjointBatch(p, [cases[d][2] for d in ds], nsteps)
+            try:
+                ab.forward(np.stack([cases[d][0] for d in ds]), np.stack([cases[d][1] for d in ds]))
+                return ds, ab.backward()
+            finally:
+                ab.close()
+
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with _TPE(args.batch_streams) as ex:
+            res = list(ex.map(run_group, groups))
+        torch.cuda.synchronize()
+        t_cb = time.perf_counter() - t0
+        same_cb = all(np.array_equal(ga[k], grads[d][0]) and np.array_equal(gp[k], grads[d][1])
+                      for ds, (ga, gp) in res for k, d in enumerate(ds))
+        conc_batched = {"value": args.designs / t_cb, "designs_per_batch": size,
+                        "concurrent_batches": args.batch_streams, "gradients_equal_batched": bool(same_cb),
+                        "method": "fv_adjoint_batch handles of designs_per_batch designs, concurrent_batches at "
+                                  "a time, each on its own stream from a host thread (creation included)"}
     # the previous method: one handle per design, `concurrent` streams
     conc = max(1, args.concurrent)
     n_conc = min(args.designs, args.conc_designs)
@@ -908,9 +938,12 @@ def designs_report(args, batch: int) -> dict:
     t_conc = time.perf_counter() - t0
     same = all(np.array_equal(conc_grads[d][0], grads[d][0]) and np.array_equal(conc_grads[d][1], grads[d][1])
                for d in range(n_conc))
+    best = conc_batched["value"] if conc_batched else args.designs / t_batched
     return {
         **_designs_fp64_check(grads, nsteps, args.seed),
-        "value": args.designs / t_batched, "unit": "gradients/s",
+        "value": max(best, args.designs / t_batched), "unit": "gradients/s",
+        "batched_sequential": {"value": args.designs / t_batched, "designs_per_batch": batch,
+                               "method": "fv_adjoint_batch handles of designs_per_batch designs, one after another"},
         "designs": args.designs, "designs_per_batch": batch, "steps": nsteps,
         "forward_plain_s": t_plain,
         "recorded_forward_s_per_design": t_fwd / args.designs,
@@ -918,6 +951,7 @@ def designs_report(args, batch: int) -> dict:
         "gradient_over_forward": t_batched / args.designs / t_plain,
         "adjoint_forward_ratio": t_bwd / args.designs / t_plain,
         "peak_adjoint_memory_gb": peak / 1e9,
+        **({"batched_concurrent": conc_batched} if conc_batched else {}),
         "streams": {"value": n_conc / t_conc, "designs": n_conc, "concurrent": conc,
                     "method": "one fv_adjoint per design, each on its own stream from a host thread"},
         "batched_gradients_equal_alone": bool(same),
@@ -971,7 +1005,9 @@ def run_designs(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": r["workload"], "designs": r["designs"], "designs_per_batch": r["designs_per_batch"]},
+        "config": {"workload": r["workload"], "designs": r["designs"], "designs_per_batch": r["designs_per_batch"],
+                   **({"concurrent_batches": args.batch_streams, "designs_per_concurrent_batch": args.stream_batch}
+                      if args.batch_streams > 1 else {})},
         "designs": r,
         "clocks": clocks,
     }
@@ -1002,6 +1038,11 @@ def main():
                     help="designs workload: designs run at a time, each on its own stream")
     ap.add_argument("--designs-per-batch", type=int, default=16,
                     help="designs workload: designs per fv_adjoint_batch (about 10 GB each at 2048x1024, 6000 steps)")
+    ap.add_argument("--batch-streams", type=int, default=2,
+                    help="designs workload: also run batches of --stream-batch designs this many at a time, "
+                         "each on its own stream")
+    ap.add_argument("--stream-batch", type=int, default=8,
+                    help="designs workload: designs per batch for --batch-streams")
     ap.add_argument("--conc-designs", type=int, default=8,
                     help="designs workload: designs run one handle per design on streams, for comparison")
     ap.add_argument("--adjoint-steps", type=int, default=0,
