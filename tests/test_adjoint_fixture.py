@@ -63,3 +63,15 @@ def test_fixture_parameters_are_the_library_defaults():
     assert config4_params().as_dict() == lib.as_dict()
     c5 = lib.replace(nx=2048, ny=1024, xmax=2047 / 24, ymax=1023 / 24, center=512.0)
     assert config5_params().as_dict() == c5.as_dict()
+
+
+def test_config5_fixture_is_complete():
+    with open(os.path.join(HERE, "golden", "adjoint_config5.json")) as f:
+        fx = json.load(f)
+    case = fx["case"]
+    assert (case["nx"], case["ny"], case["nsteps"], case["design"]) == (2048, 1024, 6000, 0)
+    fd = np.asarray(fx["fd64"])
+    assert len(fd) == len(fx["directions"]) == 4 and np.all(np.isfinite(fd)) and np.all(fd != 0)
+    assert fx["loss32"] > 0
+    z = np.load(os.path.join(HERE, "golden", "adjoint_config5_schedule.npz"))
+    assert z["dts"].shape == z["Ts"].shape == (6000,) and np.all(z["dts"] > 0) and np.all(np.diff(z["Ts"]) > 0)
