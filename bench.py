@@ -431,7 +431,9 @@ def batched_report(args) -> dict:
 
     plist = configs.batched(args.instances, seed=args.seed, exact=1)
     cells = [p.nx * p.ny for p in plist]
+    blocks = autotune.tune_batch(plist)
     b = Batch(plist)
+    b.set_launch(blocks)
     b.init_state()
     b.run(max(args.warmup, 3))
     ms_batch = b.time_run(args.steps)
@@ -451,7 +453,7 @@ def batched_report(args) -> dict:
         sim.close()
     sequential = work_seq / (ms_seq * 1e-3) / 1e9
     return {"value": batched, "unit": "Gcell-updates/s", "sequential": sequential,
-            "ratio": batched / sequential, "instances": len(plist), "cells_per_step": sum(cells),
+            "ratio": batched / sequential, "ctas": blocks, "instances": len(plist), "cells_per_step": sum(cells),
             "steps": args.steps, "ms_per_attempt": ms_batch / args.steps,
             "workload": f"{len(plist)} focused-beam simulations, sides from {list(configs.SIDES)} drawn "
                         f"independently for x and y, random physics, seed {args.seed}"}
@@ -705,7 +707,7 @@ def run_batched(args):
         "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": r["workload"], "cells_per_step": r["cells_per_step"],
-                   "sides": list(configs.SIDES), "variant": "exact"},
+                   "sides": list(configs.SIDES), "variant": "exact", "ctas": r["ctas"]},
         "sequential_plain_path": {"value": r["sequential"], "unit": "Gcell-updates/s"},
         "batched_over_sequential": r["ratio"],
         "clocks": clocks,

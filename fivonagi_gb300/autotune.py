@@ -15,7 +15,8 @@ with the same arithmetic):
 The best choice depends on the grid size. `tune` times each candidate on a
 scratch copy of the simulation with the library's own CUDA-event timing
 (fv_time_run) and caches the winner per (device, grid, variant) in a JSON
-file next to the library.
+file next to the library. `tune_batch` does the same for a batch's CTA
+count (fv_batch_set_launch).
 """
 from __future__ import annotations
 
@@ -109,6 +110,48 @@ def tune(params: FvParams, steps: int = 40, refresh: bool = False) -> Launch:
                   "ms_per_step": results[best],
                   "candidates": {f"{_abi.FV_CTA_SHAPES[c.shape]}/{c.blocks}/{'exact' if c.division else 'fma'}": v
                                  for c, v in sorted(results.items())}}
+    _store(cache)
+    return best
+
+
+BATCH_WAVES = (2, 4, 6, 8, 12, 16)
+
+
+def _batch_key(params_list, device: str) -> str:
+    import hashlib
+
+    sig = repr([(p.nx, p.ny, p.exact, p.app) for p in params_list]).encode()
+    return f"v{CACHE_VERSION}|{device}|batch|{len(params_list)}|{hashlib.sha1(sig).hexdigest()[:16]}"
+
+
+def tune_batch(params_list, steps: int = 6, refresh: bool = False) -> int:
+    """CTAs of the batched step launch for this batch of simulations
+    (cached per device and batch shape). Its simulations cost different
+    amounts per row, and more waves of CTAs even out the split at the price
+    of more warm-up rows; each candidate (BATCH_WAVES waves of the CTAs
+    resident at once) is timed on a scratch batch with the library's own
+    CUDA-event timing (fv_batch_time_run). Every count gives the same bits."""
+    from .solver import Batch
+
+    key = _batch_key(params_list, _abi.device_name())
+    cache = _load()
+    if key in cache and not refresh:
+        return int(cache[key]["blocks"])
+    b = Batch(params_list)
+    results = {}
+    try:
+        b.init_state()
+        b.run(3)
+        _, resident = b.get_launch()
+        for w in BATCH_WAVES:
+            b.set_launch(w * resident)
+            b.run(1)
+            results[w * resident] = b.time_run(steps) / steps
+    finally:
+        b.close()
+    best = min(results, key=results.get)
+    cache[key] = {"blocks": best, "ms_per_attempt": results[best],
+                  "candidates": {str(k): v for k, v in sorted(results.items())}}
     _store(cache)
     return best
 

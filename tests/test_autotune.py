@@ -50,3 +50,33 @@ def test_tuned_launch_is_cached_and_matches_the_oracle(tmp_path, monkeypatch):
     g, o = sim.get_state(), orc.get_state()
     assert all(same_values(g[f], o[f]) for f in range(3))
     sim.close()
+
+
+def test_batch_cache_key_names_the_batch_shape():
+    a = _abi.FvParams()
+    a.nx, a.ny, a.exact = 256, 512, 1
+    b = a.replace(nx=512)
+    assert autotune._batch_key([a, b], "GB300") != autotune._batch_key([b, a], "GB300")
+    assert autotune._batch_key([a, b], "GB300").startswith(f"v{autotune.CACHE_VERSION}|GB300|batch|2|")
+
+
+@pytest.mark.gpu
+def test_tuned_batch_launch_gives_the_same_bits(tmp_path, monkeypatch):
+    from fivonagi_gb300 import Batch
+    from tests.helpers import small_params
+
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "autotune.json"))
+    plist = [small_params(3, 300, 130), small_params(0, 96, 48), small_params(2, 200, 64)]
+    blocks = autotune.tune_batch(plist, steps=4)
+    assert autotune.tune_batch(plist) == blocks  # from the cache
+    states = []
+    for nb in (0, blocks):
+        b = Batch(plist)
+        b.set_launch(nb)
+        b.init_state()
+        b.run(15)
+        states.append([b.get_state(k) for k in range(len(plist))])
+        b.close()
+    for k in range(len(plist)):
+        for f in range(3):
+            np.testing.assert_array_equal(states[0][k][f], states[1][k][f])
